@@ -1,0 +1,96 @@
+/*
+ * odp_gb300.h -- entry points of libodp_gb300 beyond the reference's odp.h.
+ * None of these has a counterpart in the reference; each evaluates graphs
+ * exactly as ODP_Init_aspl_* + ODP_Set_aspl would (same diameter, sum and
+ * ASPL bits), and returns an error code instead of exiting.
+ *
+ *   ODP_Set_aspl_batch   many graphs of any size/degree/symmetry in one
+ *                        persistent launch (replayed as a CUDA graph when the
+ *                        same shapes come back)
+ *   ODPX_Batch_*         the same with an explicit, reusable plan
+ *   ODPX_Serve_*         device-resident graphs updated by 2-opt deltas,
+ *                        evaluated in continuous batches (serving mode)
+ *   ODPX_Generate_*      the reference generators on a private random stream
+ *                        (same graphs for the same seed, thread-safe)
+ */
+#ifndef ODP_GB300_H_INCLUDED
+#define ODP_GB300_H_INCLUDED
+#include <stddef.h>
+#include "odp.h"
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Error codes (0 = success). */
+#define ODPX_OK            0
+#define ODPX_ERR_INVALID   1   /* bad shape: n % s != 0, bad grid symmetry, ... */
+#define ODPX_ERR_CUDA      2   /* a CUDA call failed */
+#define ODPX_ERR_ADJACENCY 3   /* adjacency entry outside [0, n) or degree > d */
+#define ODPX_ERR_TIMEOUT   4   /* a device-side wait ran past its limit */
+#define ODPX_ERR_MEMORY    5   /* admission refused: over the memory budget */
+#define ODPX_ERR_STATE     6   /* call out of order (e.g. no plan) */
+
+/* One graph of a batch: the arguments of the matching ODP_Init_aspl_* call
+ * plus the adjacency of ODP_Set_aspl. */
+typedef struct {
+  int grid;                  /* 0: ODP_Init_aspl_general[_s], 1: ODP_Init_aspl_grid[_s] */
+  int nodes;                 /* general graphs: number of vertices */
+  int width, height;         /* grid graphs */
+  int degree;
+  int symmetries;            /* 1 for the non-_s variants */
+  const int *num_degrees;    /* as for ODP_Init_aspl_*, or NULL */
+  const int *adjacency;      /* host int[nodes/symmetries][degree] */
+} ODP_Graph;
+
+/* Evaluates `count` graphs; results written per graph.  Returns ODPX_*. */
+int ODP_Set_aspl_batch(int count, const ODP_Graph *graphs, int *diameter, long *sum, double *ASPL);
+
+/* Reusable batch plan (same shapes every run). */
+typedef struct odp_plan ODPX_Batch;
+int  ODPX_Batch_create(int count, const ODP_Graph *graphs, ODPX_Batch **batch);
+int  ODPX_Batch_run(ODPX_Batch *batch, const int *const *adjacency, int *diameter, long *sum, double *ASPL);
+void ODPX_Batch_destroy(ODPX_Batch *batch);
+/* Device time of the last run's GPU work in ms (CUDA events on the plan's
+ * stream), and the tiles the engine processed. */
+int  ODPX_Batch_time(ODPX_Batch *batch, const int *const *adjacency, int repeats, float *ms_per_run);
+/* mode 0: whole per-call sequence (upload, expand, engine, read back);
+ * mode 1: engine on resident inputs.  flush_mb > 0 overwrites a buffer of
+ * that size before each run, outside the timed interval. */
+int  ODPX_Batch_time_mode(ODPX_Batch *batch, const int *const *adjacency, int repeats, int mode, int flush_mb,
+                          float *ms_per_run);
+unsigned long long ODPX_Batch_tiles(const ODPX_Batch *batch);
+/* Introspection for benchmarks: jobs, slots, chunk width (log2 words) of graph i. */
+int  ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots, int *wc_log2, int *tile_rows);
+/* Level at which each job (graph x column chunk, plan order) of the last run
+ * finished (negative: stalled, i.e. unreachable pairs).  Returns the job count. */
+int  ODPX_Batch_job_levels(const ODPX_Batch *batch, int *levels, int max_jobs);
+/* Time limit of the engine's idle waits (default 60 s); past it the run
+ * stops with ODPX_ERR_TIMEOUT instead of waiting on. */
+void ODPX_Batch_set_wait_limit(ODPX_Batch *batch, unsigned long long ns);
+
+/* Tuning knobs for plans created after the call (0 = automatic; use_graph:
+ * -1 automatic, 0 off, 1 on). */
+void ODPX_Set_tuning(int wc_log2, int slots, int tile_rows, int l2_budget_mb, int local_kb, int use_graph);
+
+/* Drop-in introspection: the plan behind the current ODP_Init_aspl_* state. */
+ODPX_Batch *ODPX_Current_plan(void);
+
+/* Seeded generators on a private stream (bit-identical to ODP_Srand(seed)
+ * followed by the ODP_Generate_* call). */
+void ODPX_Generate_random_general_seeded(unsigned int seed, int nodes, int degree, int symmetries, int (*edge)[2]);
+void ODPX_Generate_random_grid_seeded(unsigned int seed, int width, int height, int degree, int length,
+                                      int symmetries, int (*edge)[2]);
+/* Private random streams for per-chain 2-opt proposals. */
+size_t ODPX_Rng_size(void);
+void   ODPX_Rng_seed(void *rng_state, unsigned int seed);
+int    ODPX_Rng_next(void *rng_state);
+void   ODPX_Mutate_adjacency_general_s_rng(void *rng_state, int nodes, int degree, const int *num_degrees,
+                                           int symmetries, ODP_Restore *r, int *adjacency);
+
+/* Library version string. */
+const char *ODPX_Version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,421 @@
+"""odp_gb300 -- Python host interface to libodp_gb300, the GB300 ODP library.
+
+The C library is the product: the drop-in ``odp.h`` API (ODP_Init_aspl_*,
+ODP_Set_aspl, ODP_Finalize_aspl and the graph utilities) plus the batch and
+serving extensions of ``include/odp_gb300.h``.  This module binds those C
+entry points with ctypes and mirrors them with the same names, argument
+meaning and error behaviour, so tests and benchmarks read like the
+reference's own sample programs (sample/general.c, sample/grid.c).
+
+Loading fails loudly when the shared library has not been built (there is no
+CPU fallback): run ``python -m odp_gb300.build`` or ``__graft_entry__.build()``.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libodp_gb300.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_ADJACENCY, ERR_TIMEOUT, ERR_MEMORY, ERR_STATE = range(7)
+_ERR_NAMES = {1: "invalid shape", 2: "CUDA error", 3: "adjacency out of range",
+              4: "device wait timed out", 5: "over memory budget", 6: "call out of order"}
+
+INT_MAX = 2**31 - 1
+LONG_MAX = 2**63 - 1
+
+
+class ODPError(RuntimeError):
+    def __init__(self, code, what=""):
+        super().__init__("%s failed: %s (code %d)" % (what, _ERR_NAMES.get(code, "error"), code))
+        self.code = code
+
+
+class Restore(ctypes.Structure):
+    """ODP_Restore (odp.h): the four adjacency slots a 2-opt swap rewrote."""
+    _fields_ = [("u", ctypes.c_int * 2), ("v", ctypes.c_int * 2),
+                ("u_d", ctypes.c_int * 2), ("v_d", ctypes.c_int * 2)]
+
+
+class Graph(ctypes.Structure):
+    """ODP_Graph (odp_gb300.h): one graph of a batch."""
+    _fields_ = [("grid", ctypes.c_int), ("nodes", ctypes.c_int), ("width", ctypes.c_int),
+                ("height", ctypes.c_int), ("degree", ctypes.c_int), ("symmetries", ctypes.c_int),
+                ("num_degrees", ctypes.POINTER(ctypes.c_int)), ("adjacency", ctypes.POINTER(ctypes.c_int))]
+
+
+_lib = None
+
+
+def load():
+    """Loads libodp_gb300.so (once); raises if it is missing."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libodp_gb300.so is not built (expected at %s); "
+                          "run `python -m odp_gb300.build`" % LIB_PATH)
+    lib = ctypes.CDLL(LIB_PATH)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    IP = ctypes.POINTER(ctypes.c_int)
+    sig = {
+        "ODP_Init_aspl_general": (None, [I, I, P]),
+        "ODP_Init_aspl_general_s": (None, [I, I, P, I]),
+        "ODP_Init_aspl_grid": (None, [I, I, I, P]),
+        "ODP_Init_aspl_grid_s": (None, [I, I, I, P, I]),
+        "ODP_Set_aspl": (None, [P, IP, ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_double)]),
+        "ODP_Finalize_aspl": (None, []),
+        "ODP_Srand": (None, [ctypes.c_uint]),
+        "ODP_Generate_random_general": (None, [I, I, P]),
+        "ODP_Generate_random_general_s": (None, [I, I, I, P]),
+        "ODP_Generate_random_grid": (None, [I, I, I, I, P]),
+        "ODP_Generate_random_grid_s": (None, [I, I, I, I, I, P]),
+        "ODPX_Generate_random_general_seeded": (None, [ctypes.c_uint, I, I, I, P]),
+        "ODPX_Generate_random_grid_seeded": (None, [ctypes.c_uint, I, I, I, I, I, P]),
+        "ODP_Conv_edge2adjacency_general": (None, [I, I, I, P, P]),
+        "ODP_Conv_edge2adjacency_general_s": (None, [I, I, I, P, I, P]),
+        "ODP_Conv_edge2adjacency_grid": (None, [I, I, I, I, P, P]),
+        "ODP_Conv_edge2adjacency_grid_s": (None, [I, I, I, I, P, I, P]),
+        "ODP_Conv_adjacency2edge_general": (None, [I, I, P, P, P]),
+        "ODP_Conv_adjacency2edge_general_s": (None, [I, I, P, P, I, P]),
+        "ODP_Conv_adjacency2edge_grid": (None, [I, I, I, P, P, P]),
+        "ODP_Conv_adjacency2edge_grid_s": (None, [I, I, I, P, P, I, P]),
+        "ODP_Mutate_adjacency_general": (None, [I, I, P, ctypes.POINTER(Restore), P]),
+        "ODP_Mutate_adjacency_general_s": (None, [I, I, P, I, ctypes.POINTER(Restore), P]),
+        "ODP_Mutate_adjacency_grid": (None, [I, I, I, P, I, ctypes.POINTER(Restore), P]),
+        "ODP_Mutate_adjacency_grid_s": (None, [I, I, I, P, I, I, ctypes.POINTER(Restore), P]),
+        "ODP_Restore_adjacency_general": (None, [Restore, P]),
+        "ODP_Restore_adjacency_grid": (None, [Restore, P]),
+        "ODP_Set_aspl_batch": (I, [I, ctypes.POINTER(Graph), IP, ctypes.POINTER(ctypes.c_long),
+                                   ctypes.POINTER(ctypes.c_double)]),
+        "ODPX_Batch_create": (I, [I, ctypes.POINTER(Graph), ctypes.POINTER(P)]),
+        "ODPX_Batch_run": (I, [P, ctypes.POINTER(P), IP, ctypes.POINTER(ctypes.c_long),
+                               ctypes.POINTER(ctypes.c_double)]),
+        "ODPX_Batch_destroy": (None, [P]),
+        "ODPX_Batch_time_mode": (I, [P, ctypes.POINTER(P), I, I, I, ctypes.POINTER(ctypes.c_float)]),
+        "ODPX_Batch_tiles": (ctypes.c_ulonglong, [P]),
+        "ODPX_Batch_info": (I, [P, I, IP, IP, IP, IP]),
+        "ODPX_Batch_job_levels": (I, [P, IP, I]),
+        "ODPX_Batch_set_wait_limit": (None, [P, ctypes.c_ulonglong]),
+        "ODPX_Set_tuning": (None, [I, I, I, I, I, I]),
+        "ODPX_Current_plan": (P, []),
+        "ODPX_Rng_size": (ctypes.c_size_t, []),
+        "ODPX_Rng_seed": (None, [P, ctypes.c_uint]),
+        "ODPX_Rng_next": (I, [P]),
+        "ODPX_Mutate_adjacency_general_s_rng": (None, [P, I, I, P, I, ctypes.POINTER(Restore), P]),
+        "ODPX_Version": (ctypes.c_char_p, []),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib
+
+
+def _iptr(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def _ints(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.int32)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def _check(code, what):
+    if code != OK:
+        raise ODPError(code, what)
+
+
+# --------------------------------------------------------------------------
+# Drop-in ASPL API (odp.h).
+# --------------------------------------------------------------------------
+
+def init_aspl_general(nodes, degree, num_degrees=None):
+    """ODP_Init_aspl_general."""
+    global _nd_keep
+    _nd_keep = None if num_degrees is None else _ints(num_degrees)
+    load().ODP_Init_aspl_general(nodes, degree, _iptr(_nd_keep))
+
+
+def init_aspl_general_s(nodes, degree, num_degrees, symmetries):
+    """ODP_Init_aspl_general_s."""
+    global _nd_keep
+    _nd_keep = None if num_degrees is None else _ints(num_degrees)
+    load().ODP_Init_aspl_general_s(nodes, degree, _iptr(_nd_keep), symmetries)
+
+
+def init_aspl_grid(width, height, degree, num_degrees=None):
+    """ODP_Init_aspl_grid."""
+    global _nd_keep
+    _nd_keep = None if num_degrees is None else _ints(num_degrees)
+    load().ODP_Init_aspl_grid(width, height, degree, _iptr(_nd_keep))
+
+
+def init_aspl_grid_s(width, height, degree, num_degrees, symmetries):
+    """ODP_Init_aspl_grid_s."""
+    global _nd_keep
+    _nd_keep = None if num_degrees is None else _ints(num_degrees)
+    load().ODP_Init_aspl_grid_s(width, height, degree, _iptr(_nd_keep), symmetries)
+
+
+_nd_keep = None
+
+
+def set_aspl(adjacency):
+    """ODP_Set_aspl: returns (diameter, sum, ASPL)."""
+    adj = _ints(adjacency)
+    d = ctypes.c_int()
+    s = ctypes.c_long()
+    a = ctypes.c_double()
+    load().ODP_Set_aspl(_iptr(adj), ctypes.byref(d), ctypes.byref(s), ctypes.byref(a))
+    return d.value, s.value, a.value
+
+
+def finalize_aspl():
+    """ODP_Finalize_aspl."""
+    load().ODP_Finalize_aspl()
+
+
+# --------------------------------------------------------------------------
+# Graph utilities.
+# --------------------------------------------------------------------------
+
+def srand(seed):
+    load().ODP_Srand(seed)
+
+
+def generate_random_general(nodes, degree, symmetries=1, seed=None):
+    """Edge list int32[nodes*degree/2][2] from ODP_Generate_random_general(_s).
+
+    With ``seed`` the private stream is used (same graph as ODP_Srand(seed)
+    followed by the generator); without, the libc rand() stream."""
+    lines = nodes * degree // 2
+    edge = np.zeros((lines, 2), dtype=np.int32)
+    lib = load()
+    if seed is not None:
+        lib.ODPX_Generate_random_general_seeded(seed, nodes, degree, symmetries, _iptr(edge))
+    elif symmetries == 1:
+        lib.ODP_Generate_random_general(nodes, degree, _iptr(edge))
+    else:
+        lib.ODP_Generate_random_general_s(nodes, degree, symmetries, _iptr(edge))
+    return edge
+
+
+def generate_random_grid(width, height, degree, length, symmetries=1, seed=None):
+    """Edge list from ODP_Generate_random_grid(_s) (vertex id = x*height + y)."""
+    lines = width * height * degree // 2
+    edge = np.zeros((lines, 2), dtype=np.int32)
+    lib = load()
+    if seed is not None:
+        lib.ODPX_Generate_random_grid_seeded(seed, width, height, degree, length, symmetries, _iptr(edge))
+    elif symmetries == 1:
+        lib.ODP_Generate_random_grid(width, height, degree, length, _iptr(edge))
+    else:
+        lib.ODP_Generate_random_grid_s(width, height, degree, length, symmetries, _iptr(edge))
+    return edge
+
+
+def conv_edge2adjacency_general(nodes, edge, degree, symmetries=1):
+    """ODP_Conv_edge2adjacency_general(_s): int32[nodes/s][degree], -1 padded."""
+    edge = _ints(edge)
+    adj = np.zeros((nodes // symmetries, degree), dtype=np.int32)
+    load().ODP_Conv_edge2adjacency_general_s(nodes, len(edge), degree, _iptr(edge), symmetries, _iptr(adj))
+    return adj
+
+
+def conv_edge2adjacency_grid(width, height, edge, degree, symmetries=1):
+    """ODP_Conv_edge2adjacency_grid(_s): int32[w*h/s][degree], -1 padded."""
+    edge = _ints(edge)
+    adj = np.zeros((width * height // symmetries, degree), dtype=np.int32)
+    load().ODP_Conv_edge2adjacency_grid_s(width, height, len(edge), degree, _iptr(edge), symmetries, _iptr(adj))
+    return adj
+
+
+def conv_adjacency2edge_general(nodes, degree, adjacency, symmetries=1, num_degrees=None):
+    adj = _ints(adjacency)
+    nd = None if num_degrees is None else _ints(num_degrees)
+    total = nodes * degree if nd is None else int(np.sum(nd)) * symmetries
+    edge = np.zeros((total // 2, 2), dtype=np.int32)
+    load().ODP_Conv_adjacency2edge_general_s(nodes, degree, _iptr(nd), _iptr(adj), symmetries, _iptr(edge))
+    return edge
+
+
+def conv_adjacency2edge_grid(width, height, degree, adjacency, symmetries=1, num_degrees=None):
+    adj = _ints(adjacency)
+    nd = None if num_degrees is None else _ints(num_degrees)
+    nodes = width * height
+    total = nodes * degree if nd is None else int(np.sum(nd)) * symmetries
+    edge = np.zeros((total // 2, 2), dtype=np.int32)
+    load().ODP_Conv_adjacency2edge_grid_s(width, height, degree, _iptr(nd), _iptr(adj), symmetries, _iptr(edge))
+    return edge
+
+
+def mutate_adjacency_general(nodes, degree, adjacency, symmetries=1, num_degrees=None):
+    """ODP_Mutate_adjacency_general(_s) in place; returns the Restore record."""
+    r = Restore()
+    nd = None if num_degrees is None else _ints(num_degrees)
+    load().ODP_Mutate_adjacency_general_s(nodes, degree, _iptr(nd), symmetries, ctypes.byref(r), _iptr(adjacency))
+    return r
+
+
+def mutate_adjacency_grid(width, height, degree, length, adjacency, symmetries=1, num_degrees=None):
+    r = Restore()
+    nd = None if num_degrees is None else _ints(num_degrees)
+    load().ODP_Mutate_adjacency_grid_s(width, height, degree, _iptr(nd), length, symmetries, ctypes.byref(r),
+                                       _iptr(adjacency))
+    return r
+
+
+def restore_adjacency_general(r, adjacency):
+    load().ODP_Restore_adjacency_general(r, _iptr(adjacency))
+
+
+def restore_adjacency_grid(r, adjacency):
+    load().ODP_Restore_adjacency_grid(r, _iptr(adjacency))
+
+
+class Rng:
+    """A private glibc-compatible random stream (ODPX_Rng_*)."""
+
+    def __init__(self, seed):
+        self._buf = ctypes.create_string_buffer(int(load().ODPX_Rng_size()))
+        load().ODPX_Rng_seed(self._buf, seed)
+
+    def next(self):
+        return load().ODPX_Rng_next(self._buf)
+
+    @property
+    def state(self):
+        return self._buf
+
+    def mutate_general(self, nodes, degree, adjacency, symmetries=1, num_degrees=None):
+        r = Restore()
+        nd = None if num_degrees is None else _ints(num_degrees)
+        load().ODPX_Mutate_adjacency_general_s_rng(self._buf, nodes, degree, _iptr(nd), symmetries,
+                                                   ctypes.byref(r), _iptr(adjacency))
+        return r
+
+
+# --------------------------------------------------------------------------
+# Batch API (odp_gb300.h).
+# --------------------------------------------------------------------------
+
+class GraphSpec:
+    """One graph of a batch: the ODP_Init_aspl_* arguments and an adjacency."""
+
+    def __init__(self, adjacency, nodes=0, degree=None, symmetries=1, num_degrees=None,
+                 grid=False, width=0, height=0):
+        self.grid = bool(grid)
+        self.nodes = width * height if grid else nodes
+        self.width, self.height = width, height
+        self.symmetries = symmetries
+        self.adjacency = _ints(adjacency)
+        self.degree = self.adjacency.shape[1] if degree is None else degree
+        self.num_degrees = None if num_degrees is None else _ints(num_degrees)
+
+    def to_c(self):
+        g = Graph()
+        g.grid = int(self.grid)
+        g.nodes = self.nodes
+        g.width, g.height = self.width, self.height
+        g.degree = self.degree
+        g.symmetries = self.symmetries
+        g.num_degrees = (self.num_degrees.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+                         if self.num_degrees is not None else None)
+        g.adjacency = self.adjacency.ctypes.data_as(ctypes.POINTER(ctypes.c_int))
+        return g
+
+
+def set_aspl_batch(specs):
+    """ODP_Set_aspl_batch: list of (diameter, sum, ASPL), one per spec."""
+    n = len(specs)
+    arr = (Graph * n)(*[s.to_c() for s in specs])
+    d = np.zeros(n, dtype=np.int32)
+    s = np.zeros(n, dtype=np.int64)
+    a = np.zeros(n, dtype=np.float64)
+    rc = load().ODP_Set_aspl_batch(n, arr, d.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                   s.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                                   a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+    _check(rc, "ODP_Set_aspl_batch")
+    return [(int(d[i]), int(s[i]), float(a[i])) for i in range(n)]
+
+
+class Batch:
+    """A reusable batch plan (ODPX_Batch_*): fixed shapes, new adjacency per run."""
+
+    def __init__(self, specs):
+        self.specs = list(specs)
+        n = len(self.specs)
+        arr = (Graph * n)(*[s.to_c() for s in self.specs])
+        h = ctypes.c_void_p()
+        _check(load().ODPX_Batch_create(n, arr, ctypes.byref(h)), "ODPX_Batch_create")
+        self._h = h
+        self.count = n
+
+    def _adj_ptrs(self, adjacency=None):
+        if adjacency is None:
+            adjacency = [s.adjacency for s in self.specs]
+        self._keep = [_ints(a) for a in adjacency]
+        return (ctypes.c_void_p * self.count)(*[a.ctypes.data for a in self._keep])
+
+    def run(self, adjacency=None):
+        n = self.count
+        d = np.zeros(n, dtype=np.int32)
+        s = np.zeros(n, dtype=np.int64)
+        a = np.zeros(n, dtype=np.float64)
+        rc = load().ODPX_Batch_run(self._h, self._adj_ptrs(adjacency), d.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                   s.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
+                                   a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+        _check(rc, "ODPX_Batch_run")
+        return [(int(d[i]), int(s[i]), float(a[i])) for i in range(n)]
+
+    def time(self, repeats, mode=1, flush_mb=0, adjacency=None):
+        """Average device ms per run (CUDA events on the plan's stream)."""
+        ms = ctypes.c_float()
+        rc = load().ODPX_Batch_time_mode(self._h, self._adj_ptrs(adjacency), repeats, mode, flush_mb,
+                                         ctypes.byref(ms))
+        _check(rc, "ODPX_Batch_time_mode")
+        return ms.value
+
+    def tiles(self):
+        return int(load().ODPX_Batch_tiles(self._h))
+
+    def info(self, graph=0):
+        v = [ctypes.c_int() for _ in range(4)]
+        _check(load().ODPX_Batch_info(self._h, graph, *[ctypes.byref(x) for x in v]), "ODPX_Batch_info")
+        return dict(njobs=v[0].value, nslots=v[1].value, wc_log2=v[2].value, tile_rows=v[3].value)
+
+    def job_levels(self):
+        """Per-job finishing level of the last run (plan order; negative: stalled)."""
+        n = self.info(0)["njobs"]
+        out = np.zeros(n, dtype=np.int32)
+        load().ODPX_Batch_job_levels(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+        return out
+
+    def set_wait_limit(self, ns):
+        load().ODPX_Batch_set_wait_limit(self._h, int(ns))
+
+    def close(self):
+        if self._h:
+            load().ODPX_Batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_tuning(wc_log2=0, slots=0, tile_rows=0, l2_budget_mb=0, local_kb=0, use_graph=-1):
+    """ODPX_Set_tuning: knobs for plans created afterwards (0 = automatic)."""
+    load().ODPX_Set_tuning(wc_log2, slots, tile_rows, l2_budget_mb, local_kb, use_graph)
+
+
+def version():
+    return load().ODPX_Version().decode()

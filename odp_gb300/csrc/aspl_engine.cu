@@ -1,0 +1,546 @@
+/*
+ * aspl_engine.cu -- the GB300 (sm_103a) kernels of the ODP ASPL/diameter
+ * evaluation and the thin extern "C" layer the host C driver calls.
+ *
+ * The computation is the reference's bitset BFS (aspl_cuda.cu:53-126,
+ * utils_cuda.cu:97-211): rows are vertices, bits are source vertices (the
+ * n/s base vertices of a symmetric graph), and level k sets bit (v, src)
+ * when src is within distance k of v:
+ *
+ *     P_k[v] = P_{k-1}[v] | OR_{u in N(v)} P_{k-1}[u],     P_0 = identity
+ *
+ * which is what the reference's A/B double buffer computes (its B keeps
+ * P_{k-2}, and P_{k-2}[v] | OR P_{k-1}[u] = P_k[v] because P only grows).
+ * popcount(P_k) decides termination and the sum exactly as the reference's
+ * host loop does (aspl_cuda.cu:62-82, 102-121).
+ *
+ * GB300 design, instead of the reference's per-level kernel + popcount
+ * kernel + blocking D2H copy:
+ *  - expand_kernel turns the compact adjacency (n/s rows, symmetry-relative
+ *    ids, grid rotations) into a row-space neighbour table nbr[n][dp] once
+ *    per upload; the rotation/itable arithmetic of utils_cuda.cu:3-59 and
+ *    :117-151 runs there, not once per (row, word, level).
+ *  - engine_kernel is persistent (grid = SMs x resident CTAs).  Work is a
+ *    queue of jobs = (graph, column chunk); active jobs sit in slots, each
+ *    slot runs BFS levels, and each level is split into row tiles handed out
+ *    through a 64-bit ticket (ntiles << 32 | next).  The CTA finishing a
+ *    level's last tile decides, on the device, whether the job is complete,
+ *    stalled (disconnected) or opens the next level; a finished job folds its
+ *    sum into the graph's accumulator and the slot loads the next job.  CTAs
+ *    never wait on each other except when idle (bounded by a time limit that
+ *    raises GBX_ERR_TIMEOUT).
+ *  - Level 1 is built straight from the neighbour table (no clear/identity
+ *    pass); levels >= 2 OR-gather 128-bit vectors of the d neighbour rows
+ *    (L2-only loads: the buffers are rewritten by other SMs between levels),
+ *    and the popcount is fused: warp __reduce_add_sync, one 64-bit atomic per
+ *    tile.
+ *  - A job whose level fits in one tile (small graphs) is run to completion
+ *    by the CTA that took it, with no device-wide handshake per level.
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "odp_engine.h"
+
+#define ENGINE_THREADS 256
+#define ENGINE_WARPS (ENGINE_THREADS / 32)
+
+namespace {
+
+__device__ __forceinline__ unsigned popc4(const uint4 &v)
+{
+  return __popc(v.x) + __popc(v.y) + __popc(v.z) + __popc(v.w);
+}
+
+__device__ __forceinline__ void or_into(uint4 &a, const uint4 &b)
+{
+  a.x |= b.x; a.y |= b.y; a.z |= b.z; a.w |= b.w;
+}
+
+template <typename T>
+__device__ __forceinline__ T vload(const T *p) { return *(const volatile T *)p; }
+
+__device__ __forceinline__ unsigned long long globaltimer()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+  return t;
+}
+
+/* ---------------------------------------------------------------------- */
+/* Neighbour-table expansion.                                              */
+/* ---------------------------------------------------------------------- */
+
+/* ODP_ROTATE for the grid symmetries (reference utils_cuda.cu:3-14). */
+__device__ __forceinline__ int grid_rotate(int v, int width, int height, int s, int deg)
+{
+  int x = v / height, y = v % height;
+  if(s == 2) return (width - x - 1) * height + (height - y - 1);
+  if(deg == 90)  return y * height + (height - x - 1);
+  if(deg == 180) return (height - x - 1) * height + (height - y - 1);
+  return (height - y - 1) * height + x;
+}
+
+/* Row of a base-quadrant vertex (utils_cuda.cu:16-23). */
+__device__ __forceinline__ int grid_base_row(int x, int height, int s)
+{
+  if(s == 2) return x;
+  return (x / height) * (height / 2) + x % height;
+}
+
+/* Neighbour j of global vertex v of a rotation-symmetric grid
+ * (utils_cuda.cu:25-59); -1 when the stored entry is out of range. */
+__device__ int grid_neighbour(const gbx_expand_desc &e, int v, int j)
+{
+  const int w = e.width, h = e.height, s = e.s, d = e.d, n = e.n;
+  int x = v / h, y = v % h, bw = w / 2, bh = h / 2;
+  int src_row, back;
+  if(s == 2){
+    if(x < bw){ src_row = v; back = 0; }
+    else      { src_row = grid_rotate(v, w, h, s, 180); back = 180; }
+  }
+  else{
+    if(x < bw && y < bh)  { src_row = grid_base_row(v, h, s); back = 0; }
+    else if(x < bw)       { src_row = grid_base_row(grid_rotate(v, w, h, s, 270), h, s); back = 90; }
+    else if(y >= bh)      { src_row = grid_base_row(grid_rotate(v, w, h, s, 180), h, s); back = 180; }
+    else                  { src_row = grid_base_row(grid_rotate(v, w, h, s, 90), h, s); back = 270; }
+  }
+  int a = e.adj[(size_t)src_row * d + j];
+  if(a < 0 || a >= n) return -1;
+  return back ? grid_rotate(a, w, h, s, back) : a;
+}
+
+__global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int ndesc, long long total,
+                              unsigned int *err)
+{
+  for(long long gv = blockIdx.x * (long long)blockDim.x + threadIdx.x; gv < total;
+      gv += (long long)gridDim.x * blockDim.x){
+    int lo = 0, hi = ndesc - 1;
+    while(lo < hi){
+      int mid = (lo + hi + 1) >> 1;
+      if(descs[mid].first_vertex <= gv) lo = mid; else hi = mid - 1;
+    }
+    const gbx_expand_desc &e = descs[lo];
+    const int v = (int)(gv - e.first_vertex);
+    const int n = e.n, d = e.d, dp = e.dp;
+    int deg = e.ndeg ? e.ndeg[v] : d;
+    if(deg < 0 || deg > d){ atomicOr(err, GBX_ERR_BAD_ADJ); deg = deg < 0 ? 0 : d; }
+    const int row = e.grid_s ? e.itable[v] : v;
+    int *out = e.nbr + (size_t)row * dp;
+    const int base = n / e.s;
+    const int m = v % base, shift = (v / base) * base;
+    for(int j = 0; j < dp; j++){
+      int nb = -1;
+      if(j < deg){
+        if(e.grid_s){
+          int u = grid_neighbour(e, v, j);
+          if(u < 0) atomicOr(err, GBX_ERR_BAD_ADJ);
+          else nb = e.itable[u];
+        }
+        else{
+          int a = e.adj[(size_t)m * d + j];
+          if(a < 0 || a >= n) atomicOr(err, GBX_ERR_BAD_ADJ);
+          else{ nb = a + shift; if(nb >= n) nb -= n; }
+        }
+      }
+      out[j] = nb;
+    }
+  }
+}
+
+/* ---------------------------------------------------------------------- */
+/* Row passes.  WC = uint64 words per row of the chunk (a power of two).   */
+/* A row is covered by G lanes, each holding V 16-byte vectors.            */
+/* ---------------------------------------------------------------------- */
+
+template <int WC>
+struct RowShape {
+  static constexpr int VPR = WC / 2;                 /* uint4 vectors per row */
+  static constexpr int G = VPR < 32 ? VPR : 32;      /* lanes per row */
+  static constexpr int V = VPR / G;                  /* vectors per lane */
+  static constexpr int RPW = 32 / G;                 /* rows per warp pass */
+};
+
+/* Set local source bit b (0 <= b < nsrc) if it lands in this lane's vectors. */
+template <int WC>
+__device__ __forceinline__ void mark_source(uint4 (&acc)[RowShape<WC>::V], int b, int nsrc, int gl)
+{
+  typedef RowShape<WC> S;
+  if((unsigned)b >= (unsigned)nsrc) return;
+  const int vec = b >> 7;
+  const unsigned bit = 1u << (b & 31);
+  const int comp = (b >> 5) & 3;
+#pragma unroll
+  for(int k = 0; k < S::V; k++){
+    if(vec == gl + k * S::G){
+      acc[k].x |= (comp == 0) ? bit : 0u;
+      acc[k].y |= (comp == 1) ? bit : 0u;
+      acc[k].z |= (comp == 2) ? bit : 0u;
+      acc[k].w |= (comp == 3) ? bit : 0u;
+    }
+  }
+}
+
+/* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources. */
+template <int WC>
+__device__ unsigned rows_level1(const gbx_job &jb, unsigned long long *Y, int r0, int r1)
+{
+  typedef RowShape<WC> S;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / S::G, gl = lane % S::G;
+  const int dp = jb.dp, src0 = jb.src0, nsrc = jb.nsrc;
+  unsigned cnt = 0;
+  for(int row = r0 + warp * S::RPW + sub; row < r1; row += ENGINE_WARPS * S::RPW){
+    uint4 acc[S::V];
+#pragma unroll
+    for(int k = 0; k < S::V; k++) acc[k] = make_uint4(0u, 0u, 0u, 0u);
+    mark_source<WC>(acc, row - src0, nsrc, gl);
+    const int4 *ip = reinterpret_cast<const int4 *>(jb.nbr + (size_t)row * dp);
+    for(int j = 0; j < (dp >> 2); j++){
+      int4 q = __ldg(ip + j);
+      mark_source<WC>(acc, q.x - src0, nsrc, gl);
+      mark_source<WC>(acc, q.y - src0, nsrc, gl);
+      mark_source<WC>(acc, q.z - src0, nsrc, gl);
+      mark_source<WC>(acc, q.w - src0, nsrc, gl);
+    }
+    uint4 *yr = reinterpret_cast<uint4 *>(Y + (size_t)row * WC);
+#pragma unroll
+    for(int k = 0; k < S::V; k++){
+      __stcg(yr + gl + k * S::G, acc[k]);
+      cnt += popc4(acc[k]);
+    }
+  }
+  return cnt;
+}
+
+/* Level k >= 2: P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]]. */
+template <int WC>
+__device__ unsigned rows_levelk(const gbx_job &jb, const unsigned long long *X, unsigned long long *Y,
+                                int r0, int r1)
+{
+  typedef RowShape<WC> S;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / S::G, gl = lane % S::G;
+  const int dp = jb.dp;
+  const uint4 *Xv = reinterpret_cast<const uint4 *>(X);
+  unsigned cnt = 0;
+  for(int row = r0 + warp * S::RPW + sub; row < r1; row += ENGINE_WARPS * S::RPW){
+    uint4 acc[S::V];
+    const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
+#pragma unroll
+    for(int k = 0; k < S::V; k++) acc[k] = __ldcg(xr + k * S::G);
+    const int4 *ip = reinterpret_cast<const int4 *>(jb.nbr + (size_t)row * dp);
+#pragma unroll 2
+    for(int j = 0; j < (dp >> 2); j++){
+      const int4 q = __ldg(ip + j);
+      uint4 t[4][S::V];
+      const int idx[4] = {q.x, q.y, q.z, q.w};
+#pragma unroll
+      for(int i = 0; i < 4; i++){
+        const uint4 *nr = Xv + (size_t)(idx[i] < 0 ? 0 : idx[i]) * S::VPR + gl;
+#pragma unroll
+        for(int k = 0; k < S::V; k++)
+          t[i][k] = (idx[i] >= 0) ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+      }
+#pragma unroll
+      for(int i = 0; i < 4; i++)
+#pragma unroll
+        for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
+    }
+    uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
+#pragma unroll
+    for(int k = 0; k < S::V; k++){
+      __stcg(yr + k * S::G, acc[k]);
+      cnt += popc4(acc[k]);
+    }
+  }
+  return cnt;
+}
+
+__device__ unsigned run_rows(const gbx_job &jb, int level, const unsigned long long *X, unsigned long long *Y,
+                             int r0, int r1)
+{
+#define ODP_WC_CASE(L) case L: return level == 1 ? rows_level1<(1 << L)>(jb, Y, r0, r1) \
+                                                 : rows_levelk<(1 << L)>(jb, X, Y, r0, r1);
+  switch(jb.wc_log2){
+    ODP_WC_CASE(1) ODP_WC_CASE(2) ODP_WC_CASE(3) ODP_WC_CASE(4)
+    ODP_WC_CASE(5) ODP_WC_CASE(6) ODP_WC_CASE(7) ODP_WC_CASE(8)
+    default: return 0;
+  }
+#undef ODP_WC_CASE
+}
+
+/* ---------------------------------------------------------------------- */
+/* Persistent engine.                                                      */
+/* ---------------------------------------------------------------------- */
+
+__global__ void __launch_bounds__(ENGINE_THREADS)
+engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int nslots, gbx_ctrl *ctrl,
+              gbx_graph_acc *acc, int *job_levels, unsigned long long spin_limit_ns)
+{
+  __shared__ gbx_job sh_job;
+  __shared__ int sh_state, sh_slot, sh_tile, sh_level;
+  __shared__ unsigned long long *sh_buf0, *sh_buf1;
+  __shared__ unsigned sh_warp[ENGINE_WARPS];
+
+  int cursor = blockIdx.x % nslots;
+  unsigned long long idle_since = 0;
+
+  for(;;){
+    if(threadIdx.x == 0){
+      int state = 0;
+      for(int i = 0; i < nslots && state == 0; i++){
+        int si = cursor + i;
+        if(si >= nslots) si -= nslots;
+        gbx_slot *sl = &slots[si];
+        unsigned long long t = vload(&sl->ticket);
+        if((unsigned)t >= (unsigned)(t >> 32)) continue;
+        t = atomicAdd(&sl->ticket, 1ull);
+        if((unsigned)t >= (unsigned)(t >> 32)) continue;
+        __threadfence();                               /* acquire the level's inputs */
+        sh_slot = si;
+        sh_tile = (int)(unsigned)t;
+        sh_level = vload(&sl->level);
+        sh_job = jobs[vload(&sl->job)];
+        sh_buf0 = vload(&sl->buf0);
+        sh_buf1 = vload(&sl->buf1);
+        cursor = si;
+        state = 1;
+      }
+      if(state == 0){
+        if(vload(&ctrl->retired) >= (unsigned)nslots || (vload(&ctrl->error) & GBX_ERR_TIMEOUT)){
+          state = 2;
+        }
+        else{
+          unsigned long long now = globaltimer();
+          if(idle_since == 0) idle_since = now;
+          if(now - idle_since > spin_limit_ns){
+            atomicOr(&ctrl->error, GBX_ERR_TIMEOUT);
+            state = 2;
+          }
+          else __nanosleep(256);
+        }
+      }
+      else idle_since = 0;
+      sh_state = state;
+    }
+    __syncthreads();
+    const int state = sh_state;
+    if(state == 2) return;
+    if(state == 0){ __syncthreads(); continue; }
+
+    const gbx_job jb = sh_job;
+    const int si = sh_slot;
+    gbx_slot *sl = &slots[si];
+    unsigned long long *buf0 = sh_buf0, *buf1 = sh_buf1;
+    int level = sh_level, tile = sh_tile;
+    __syncthreads();
+
+    for(;;){
+      /* level k writes buffer k&1 and reads buffer (k-1)&1 */
+      const unsigned long long *X = (level & 1) ? buf0 : buf1;
+      unsigned long long *Y = (level & 1) ? buf1 : buf0;
+      const int r0 = tile * jb.tile_rows;
+      const int r1 = min(r0 + jb.tile_rows, jb.n);
+      unsigned cnt = run_rows(jb, level, X, Y, r0, r1);
+      cnt = __reduce_add_sync(0xffffffffu, cnt);
+      if((threadIdx.x & 31) == 0) sh_warp[threadIdx.x >> 5] = cnt;
+      __threadfence();                                 /* release this thread's row writes */
+      __syncthreads();
+      if(threadIdx.x == 0){
+        unsigned long long c_tile = 0;
+        for(int w = 0; w < ENGINE_WARPS; w++) c_tile += sh_warp[w];
+        atomicAdd(&sl->count, c_tile);
+        atomicAdd(&ctrl->tiles, 1ull);
+        __threadfence();
+        unsigned old = atomicAdd(&sl->done, 1u);
+        int next = 0;
+        if(old + 1 == (unsigned)jb.ntiles){           /* this CTA closes the level */
+          __threadfence();
+          const unsigned long long c = vload(&sl->count);
+          const unsigned long long full = (unsigned long long)jb.n * (unsigned long long)jb.nsrc;
+          const bool complete = (c == full);
+          const bool stalled = !complete && (c == vload(&sl->prev) || level >= jb.n);
+          if(!complete && !stalled){
+            sl->sum += (long long)(full - c) * jb.sym;
+            sl->prev = c;
+            sl->count = 0;
+            sl->done = 0;
+            sl->level = level + 1;
+            if(jb.ntiles == 1){ next = 1; sh_level = level + 1; }
+            else{
+              __threadfence();
+              atomicExch(&sl->ticket, (unsigned long long)jb.ntiles << 32);
+            }
+          }
+          else{
+            gbx_graph_acc *ga = &acc[jb.graph];
+            job_levels[sl->job] = stalled ? -level : level;
+            atomicAdd(&ga->sum, (unsigned long long)sl->sum);
+            atomicMax(&ga->levels, level);
+            if(stalled) atomicOr(&ga->flags, 1);
+            unsigned j = atomicAdd(&ctrl->next_job, 1u);
+            if(j < (unsigned)njobs){
+              const gbx_job nj = jobs[j];
+              sl->job = (int)j;
+              sl->level = 1;
+              sl->count = 0;
+              sl->done = 0;
+              sl->prev = (unsigned long long)nj.nsrc;
+              sl->sum = ((long long)nj.n * nj.nsrc - nj.nsrc) * nj.sym;
+              __threadfence();
+              atomicExch(&sl->ticket, (unsigned long long)nj.ntiles << 32);
+            }
+            else{
+              atomicExch(&sl->ticket, 0ull);
+              __threadfence();
+              atomicAdd(&ctrl->retired, 1u);
+            }
+          }
+        }
+        sh_state = next;
+      }
+      __syncthreads();
+      const int more = sh_state;
+      level = sh_level;
+      tile = 0;
+      __syncthreads();
+      if(!more) break;
+    }
+  }
+}
+
+int g_engine_blocks = 0;
+
+}  // namespace
+
+/* ---------------------------------------------------------------------- */
+/* extern "C" layer.                                                       */
+/* ---------------------------------------------------------------------- */
+
+extern "C" {
+
+int gbx_device_init(int *sm_count)
+{
+  cudaError_t e = cudaFree(0);
+  if(e != cudaSuccess) return (int)e;
+  int dev = 0;
+  e = cudaGetDevice(&dev);
+  if(e != cudaSuccess) return (int)e;
+  int sms = 0;
+  e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if(e != cudaSuccess) return (int)e;
+  if(sm_count) *sm_count = sms;
+  if(g_engine_blocks == 0){
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, 0);
+    if(e != cudaSuccess) return (int)e;
+    if(per_sm < 1) per_sm = 1;
+    g_engine_blocks = per_sm * sms;
+  }
+  return 0;
+}
+
+int gbx_engine_blocks(void) { return g_engine_blocks; }
+
+int gbx_malloc(void **p, size_t bytes) { return (int)cudaMalloc(p, bytes ? bytes : 256); }
+int gbx_free(void *p) { return p ? (int)cudaFree(p) : 0; }
+int gbx_host_alloc(void **p, size_t bytes) { return (int)cudaMallocHost(p, bytes ? bytes : 64); }
+int gbx_host_free(void *p) { return p ? (int)cudaFreeHost(p) : 0; }
+
+int gbx_stream_create(void **stream)
+{
+  cudaStream_t s;
+  cudaError_t e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+  *stream = (void *)s;
+  return (int)e;
+}
+
+int gbx_stream_destroy(void *stream) { return (int)cudaStreamDestroy((cudaStream_t)stream); }
+
+int gbx_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream)
+{
+  return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream);
+}
+
+int gbx_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream)
+{
+  return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream);
+}
+
+int gbx_memset(void *dst, int value, size_t bytes, void *stream)
+{
+  return (int)cudaMemsetAsync(dst, value, bytes, (cudaStream_t)stream);
+}
+
+int gbx_stream_sync(void *stream) { return (int)cudaStreamSynchronize((cudaStream_t)stream); }
+
+const char *gbx_error_string(int err) { return cudaGetErrorString((cudaError_t)err); }
+
+int gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices, unsigned int *d_error,
+               void *stream)
+{
+  if(total_vertices <= 0) return 0;
+  long long blocks = (total_vertices + 255) / 256;
+  if(blocks > 65535LL * 8) blocks = 65535LL * 8;
+  expand_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(d_descs, ndesc, total_vertices, d_error);
+  return (int)cudaGetLastError();
+}
+
+int gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots, gbx_ctrl *d_ctrl,
+                      gbx_graph_acc *d_acc, int *d_job_levels, unsigned long long spin_limit_ns, int blocks,
+                      void *stream)
+{
+  if(njobs <= 0 || nslots <= 0) return 0;
+  if(blocks <= 0) blocks = g_engine_blocks > 0 ? g_engine_blocks : 1;
+  engine_kernel<<<blocks, ENGINE_THREADS, 0, (cudaStream_t)stream>>>(d_jobs, njobs, d_slots, nslots, d_ctrl,
+                                                                     d_acc, d_job_levels, spin_limit_ns);
+  return (int)cudaGetLastError();
+}
+
+int gbx_capture_begin(void *stream)
+{
+  return (int)cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal);
+}
+
+int gbx_capture_end(void *stream, void **graph_exec)
+{
+  cudaGraph_t g;
+  cudaError_t e = cudaStreamEndCapture((cudaStream_t)stream, &g);
+  if(e != cudaSuccess) return (int)e;
+  cudaGraphExec_t ge;
+  e = cudaGraphInstantiate(&ge, g, 0);
+  cudaGraphDestroy(g);
+  if(e != cudaSuccess) return (int)e;
+  *graph_exec = (void *)ge;
+  return 0;
+}
+
+int gbx_graph_launch(void *graph_exec, void *stream)
+{
+  return (int)cudaGraphLaunch((cudaGraphExec_t)graph_exec, (cudaStream_t)stream);
+}
+
+int gbx_graph_destroy(void *graph_exec)
+{
+  return graph_exec ? (int)cudaGraphExecDestroy((cudaGraphExec_t)graph_exec) : 0;
+}
+
+int gbx_event_create(void **ev)
+{
+  cudaEvent_t e;
+  cudaError_t r = cudaEventCreate(&e);
+  *ev = (void *)e;
+  return (int)r;
+}
+
+int gbx_event_destroy(void *ev) { return (int)cudaEventDestroy((cudaEvent_t)ev); }
+int gbx_event_record(void *ev, void *stream) { return (int)cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream); }
+
+int gbx_event_elapsed_ms(void *start, void *stop, float *ms)
+{
+  cudaError_t e = cudaEventSynchronize((cudaEvent_t)stop);
+  if(e != cudaSuccess) return (int)e;
+  return (int)cudaEventElapsedTime(ms, (cudaEvent_t)start, (cudaEvent_t)stop);
+}
+
+}  /* extern "C" */

@@ -1,0 +1,111 @@
+/*
+ * odp_engine.h -- the thin C ABI between the host C driver (odp_aspl.c,
+ * odp_batch.c, odp_serve.c) and the CUDA layer (aspl_engine.cu).
+ * Plain pointers and sizes only; every device pointer here was allocated by
+ * gbx_malloc.  All calls are asynchronous on the given stream unless named
+ * *_sync.  Return values are cudaError_t codes (0 = success).
+ */
+#ifndef ODP_ENGINE_H
+#define ODP_ENGINE_H
+#include <stddef.h>
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One graph whose compact adjacency is turned into a row-space neighbour
+ * table nbr[n][dp]: row r lists the rows of r's neighbours, -1 padded. */
+typedef struct {
+  const int *adj;          /* device int[n/s][d] as passed to ODP_Set_aspl */
+  const int *ndeg;         /* device int[n] per-vertex degree, or NULL (regular) */
+  const int *itable;       /* device int[n] vertex -> row (grid symmetry), or NULL */
+  int *nbr;                /* device out int[n][dp] */
+  int n, d, dp, s;
+  int width, height;       /* grid symmetry only */
+  int grid_s;              /* 1: rows are itable-permuted, grid rotation rules */
+  int pad;
+  long long first_vertex;  /* prefix of n over the descriptors before this one */
+} gbx_expand_desc;
+
+/* One (graph, column chunk) BFS job: sources [src0, src0 + nsrc). */
+typedef struct {
+  const int *nbr;          /* device int[n][dp] */
+  int n, dp;
+  int wc_log2;             /* words (uint64) per row in this chunk = 1 << wc_log2, >= 1 */
+  int src0, nsrc;
+  int sym;                 /* symmetries: sums are scaled by it */
+  int graph;               /* index into the graph accumulators */
+  int tile_rows, ntiles;
+  int pad[3];
+} gbx_job;
+
+/* Per-slot mutable state, one 128-byte line each. */
+typedef struct {
+  unsigned long long ticket;   /* (ntiles << 32) | next tile */
+  unsigned int done;           /* tiles finished at the current level */
+  int job;                     /* job index */
+  int level;                   /* BFS level being computed (>= 1) */
+  int pad0;
+  unsigned long long count;    /* bits set so far at this level */
+  unsigned long long prev;     /* bits set at the previous level */
+  long long sum;               /* this job's share of the ordered distance sum */
+  unsigned long long *buf0, *buf1;
+  unsigned long long pad1[8];
+} gbx_slot;
+
+typedef struct {
+  unsigned int next_job;       /* next job index to load into a freed slot */
+  unsigned int retired;        /* slots with no job left */
+  unsigned int error;          /* GBX_ERR_* bits */
+  unsigned int pad;
+  unsigned long long tiles;    /* tiles processed */
+  unsigned long long pad1[5];  /* 64 bytes */
+} gbx_ctrl;
+
+typedef struct {
+  unsigned long long sum;      /* ordered distance sum (before halving) */
+  int levels;                  /* max over chunks of the level that completed */
+  int flags;                   /* 1: some chunk stalled (disconnected) */
+} gbx_graph_acc;
+
+#define GBX_ERR_BAD_ADJ   1u   /* adjacency entry outside [0, n) */
+#define GBX_ERR_TIMEOUT   2u   /* an idle wait exceeded its time limit */
+
+/* Device / memory / stream plumbing. */
+int  gbx_device_init(int *sm_count);
+int  gbx_malloc(void **p, size_t bytes);
+int  gbx_free(void *p);
+int  gbx_host_alloc(void **p, size_t bytes);
+int  gbx_host_free(void *p);
+int  gbx_stream_create(void **stream);
+int  gbx_stream_destroy(void *stream);
+int  gbx_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
+int  gbx_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int  gbx_memset(void *dst, int value, size_t bytes, void *stream);
+int  gbx_stream_sync(void *stream);
+const char *gbx_error_string(int err);
+
+/* Kernels. */
+int  gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices,
+                unsigned int *d_error, void *stream);
+int  gbx_engine_blocks(void);          /* persistent grid size (SMs x resident CTAs) */
+int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots,
+                       gbx_ctrl *d_ctrl, gbx_graph_acc *d_acc, int *d_job_levels,
+                       unsigned long long spin_limit_ns, int blocks, void *stream);
+
+/* CUDA graphs: capture everything issued on `stream` between begin and end. */
+int  gbx_capture_begin(void *stream);
+int  gbx_capture_end(void *stream, void **graph_exec);
+int  gbx_graph_launch(void *graph_exec, void *stream);
+int  gbx_graph_destroy(void *graph_exec);
+
+/* Timing with CUDA events on a stream. */
+int  gbx_event_create(void **ev);
+int  gbx_event_destroy(void *ev);
+int  gbx_event_record(void *ev, void *stream);
+int  gbx_event_elapsed_ms(void *start, void *stop, float *ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

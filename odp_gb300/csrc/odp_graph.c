@@ -1,0 +1,1026 @@
+/*
+ * odp_graph.c -- the graph utilities that sit on either side of the ASPL hot
+ * path: seeded random generators, edge-list <-> adjacency conversion, and the
+ * 2-opt Mutate/Restore edge swaps that simulated-annealing clients issue
+ * between ASPL evaluations.
+ *
+ * These are the odp.h utility entry points that the reference ships inside
+ * every libodp*.a next to the ASPL driver (utils.c).  The generators must
+ * reproduce the reference's graphs exactly for a given seed, which fixes the
+ * order of every random draw and every accept/reject decision; the code below
+ * restates those steps (cited per function) in our own structure.  Two
+ * deliberate differences, neither visible in the results:
+ *   - the random stream is an explicit odp_rng (odp_rng.h), so graphs can be
+ *     generated concurrently (ODPX_* seeded variants); the public ODP_*
+ *     functions bind it to libc rand() exactly like the reference;
+ *   - the reverse-slot search of a 2-opt proposal (get_degree_index_*) is
+ *     done only once a proposal is known to be accepted: it draws no random
+ *     numbers, so skipping it for rejected proposals changes nothing but time.
+ *
+ * Errors print to stderr and exit(1), as the reference's ERROR macro does
+ * (common.h:32).
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <stdbool.h>
+#include <math.h>
+#include "odp_rng.h"
+#include "odp_internal.h"
+
+#define ODP_FAIL(...) do{ fprintf(stderr, __VA_ARGS__); exit(1); }while(0)
+#define GEN_ITERS 10          /* GEN_GRAPH_ITERS, parameter.h:17 */
+#define UNSET (-1)            /* NOT_DEFINED, common.h:41 */
+
+/* ------------------------------------------------------------------------ */
+/* Index arithmetic shared by the general (circulant) and grid symmetries.   */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {              /* a symmetric general graph: n vertices, s orbits */
+  int n, d, s, base;          /* base = n / s rows stored */
+  const int *ndeg;            /* per base row degree, or NULL (regular) */
+  int *adj;                   /* int[base][d] */
+} gen_ctx;
+
+typedef struct {              /* a (possibly rotation-symmetric) grid graph */
+  int w, h, d, s, len, n;
+  int bw, bh;                 /* base block: x < bw, y < bh */
+  const int *ndeg;            /* per local row degree, or NULL */
+  int *adj;                   /* int[n/s][d], rows in local-index order */
+  const int *xy;              /* optional (x, y) per vertex: saves divisions */
+} grid_ctx;
+
+static inline int wrap(int x, int n)            /* NORM, utils.c:171-177 */
+{
+  while(x < 0 || x >= n) x = (x < 0) ? x + n : x - n;
+  return x;
+}
+
+/* adjacency[v][j] of the expanded general graph (GLOBAL_ADJ_GENERAL, utils.c:180-186) */
+static inline int gen_nbr(const gen_ctx *g, int v, int j)
+{
+  return wrap(g->adj[(size_t)(v % g->base) * g->d + j] + (v / g->base) * g->base, g->n);
+}
+
+/* value to store in row of `pos` so that it names global vertex v (LOCAL_INDEX_GENERAL, utils.c:266-270) */
+static inline int gen_rel(const gen_ctx *g, int v, int pos)
+{
+  return wrap(v - (pos / g->base) * g->base, g->n);
+}
+
+static inline bool gen_is_antipodal(const gen_ctx *g, int u, int v)   /* IS_DIAMETER_GENERAL, utils.c:96-102 */
+{
+  return (g->s % 2 == 0) && abs(u - v) == g->n / 2;
+}
+
+static inline int gen_deg(const gen_ctx *g, int v)
+{
+  return g->ndeg ? g->ndeg[v % g->base] : g->d;
+}
+
+/* The slot of v's row that points back at u (get_degree_index_general, utils.c:509-532). */
+static int gen_back_slot(const gen_ctx *g, int u, int v, int u_slot)
+{
+  if(u == v){
+    int dd = gen_deg(g, v);
+    for(int i = 0; i < dd; i++)
+      if(gen_nbr(g, v, i) == u && i != u_slot) return i;
+  }
+  else if(gen_is_antipodal(g, u, v)){
+    return u_slot;
+  }
+  else{
+    int dd = gen_deg(g, v);
+    for(int i = 0; i < dd; i++)
+      if(gen_nbr(g, v, i) == u) return i;
+  }
+  ODP_FAIL("Something Wrong ! [id=4]\n");
+}
+
+/* Two edges that are images of each other under the rotation (check_rotated_edges_overlap_general, utils.c:603-621). */
+static bool gen_same_orbit(const gen_ctx *g, int u0, int v0, int u1, int v1)
+{
+  int n = g->n;
+  int d0 = (u0 > v0) ? v0 - u0 + n : v0 - u0;
+  int d1 = (u1 > v1) ? v1 - u1 + n : v1 - u1;
+  int d2 = (u1 < v1) ? u1 - v1 + n : u1 - v1;
+  if(d0 == d1 && u0 % g->base == u1 % g->base) return true;
+  if(d0 == d2 && u0 % g->base == v1 % g->base) return true;
+  return false;
+}
+
+static inline void gen_put(gen_ctx *g, int v, int slot, int value)
+{
+  g->adj[(size_t)(v % g->base) * g->d + slot] = value;
+}
+
+static void fill_restore(ODP_Restore *r, const int u[2], const int us[2], const int v[2], const int vs[2])
+{
+  if(!r) return;
+  for(int i = 0; i < 2; i++){
+    r->u[i] = u[i]; r->v[i] = v[i]; r->u_d[i] = us[i]; r->v_d[i] = vs[i];
+  }
+}
+
+/* Rotate a single edge to another orbit position (mutate_adjacency_1opt_general_s, utils.c:572-601). */
+static bool gen_one_opt(odp_rng *rng, gen_ctx *g, int u, int us)
+{
+  int base = g->base, s = g->s, n = g->n;
+  int v = gen_nbr(g, u, us);
+  if(gen_is_antipodal(g, u, v)) return false;
+  int vs = gen_back_slot(g, u, v, us);
+  int nv;
+  if((u - v) % base == 0){
+    if(s <= 4) return false;
+    for(;;){
+      nv = v + base * odp_rng_below(rng, s);
+      if(u == nv || v == nv) continue;
+      if(wrap(u - v, n) == wrap(nv - u, n)) continue;
+      if(n % 2 == 1) break;
+      if((u - nv) % (n / 2) != 0) break;
+    }
+  }
+  else{
+    int k = (s % 2 == 1) ? odp_rng_below(rng, s - 1) : odp_rng_below(rng, s);
+    nv = (k != s - 1) ? v + base * (k + 1) : u + base * (s / 2);
+  }
+  int nu = v - (nv - u);
+  int a = gen_rel(g, nv, u), b = gen_rel(g, nu, v);
+  gen_put(g, u, us, a);
+  gen_put(g, v, vs, b);
+  return true;
+}
+
+/* One 2-opt attempt on a general(_s) graph (mutate_adjacency_2opt_general_s, utils.c:623-750).
+ * Returns false when the attempt is rejected; the caller retries. */
+static bool gen_two_opt(odp_rng *rng, gen_ctx *g, ODP_Restore *r)
+{
+  int u[2], v[2], us[2], vs[2];
+  const int n = g->n;
+  for(;;){
+    u[0] = odp_rng_below(rng, n);
+    u[1] = odp_rng_below(rng, n);
+    if(u[0] == u[1]) continue;
+    us[0] = odp_rng_below(rng, gen_deg(g, u[0]));
+    v[0] = gen_nbr(g, u[0], us[0]);
+    if(v[0] == u[1]) continue;
+    us[1] = odp_rng_below(rng, gen_deg(g, u[1]));
+    v[1] = gen_nbr(g, u[1], us[1]);
+    if(v[1] == u[0] || v[0] == v[1]) continue;
+    break;
+  }
+  vs[0] = gen_back_slot(g, u[0], v[0], us[0]);
+  vs[1] = gen_back_slot(g, u[1], v[1], us[1]);
+  fill_restore(r, u, us, v, vs);
+
+  bool a0 = gen_is_antipodal(g, u[0], v[0]), a1 = gen_is_antipodal(g, u[1], v[1]);
+  if(a0 && a1){
+    if((u[0] - u[1]) % g->base == 0) return false;
+    int t0, t1;
+    if(odp_rng_below(rng, 2)){ t0 = gen_rel(g, u[1], u[0]); t1 = gen_rel(g, u[0], u[1]); }
+    else                     { t0 = gen_rel(g, v[1], u[0]); t1 = gen_rel(g, v[0], u[1]); }
+    gen_put(g, u[0], us[0], t0);
+    gen_put(g, u[1], us[1], t1);
+    return true;
+  }
+  if(a0 || a1){
+    if(a1){
+      int t;
+      t = u[0]; u[0] = u[1]; u[1] = t;
+      t = us[0]; us[0] = us[1]; us[1] = t;
+      t = v[0]; v[0] = v[1]; v[1] = t;
+      t = vs[0]; vs[0] = vs[1]; vs[1] = t;
+    }
+    int opp = n / 2, k = odp_rng_below(rng, 4), t[4];
+    switch(k){
+    case 0:
+      t[0] = gen_rel(g, v[1], u[0]);        t[1] = gen_rel(g, u[1] + opp, u[1]);
+      t[2] = gen_rel(g, v[1] + opp, v[0]);  t[3] = gen_rel(g, u[0], v[1]);
+      break;
+    case 1:
+      t[0] = gen_rel(g, v[1] + opp, u[0]);  t[1] = gen_rel(g, u[1] + opp, u[1]);
+      t[2] = gen_rel(g, v[1], v[0]);        t[3] = gen_rel(g, v[0], v[1]);
+      break;
+    case 2:
+      t[0] = gen_rel(g, u[1], u[0]);        t[1] = gen_rel(g, u[0], u[1]);
+      t[2] = gen_rel(g, u[1] + opp, v[0]);  t[3] = gen_rel(g, v[1] + opp, v[1]);
+      break;
+    default:
+      t[0] = gen_rel(g, u[1] + opp, u[0]);  t[1] = gen_rel(g, v[0], u[1]);
+      t[2] = gen_rel(g, u[1], v[0]);        t[3] = gen_rel(g, v[1] + opp, v[1]);
+      break;
+    }
+    gen_put(g, u[0], us[0], t[0]);
+    gen_put(g, u[1], us[1], t[1]);
+    gen_put(g, v[0], vs[0], t[2]);
+    gen_put(g, v[1], vs[1], t[3]);
+    return true;
+  }
+
+  if(gen_same_orbit(g, u[0], v[0], u[1], v[1]))
+    return gen_one_opt(rng, g, u[0], us[0]);
+
+  int t[4];
+  if(odp_rng_below(rng, 2)){            /* u0--v1, v0--u1 */
+    if(gen_is_antipodal(g, u[0], v[1]) || gen_is_antipodal(g, v[0], u[1])) return false;
+    if(gen_same_orbit(g, u[0], v[1], v[0], u[1])) return false;
+    t[0] = gen_rel(g, v[1], u[0]); t[1] = gen_rel(g, v[0], u[1]);
+    t[2] = gen_rel(g, u[1], v[0]); t[3] = gen_rel(g, u[0], v[1]);
+  }
+  else{                                 /* u0--u1, v0--v1 */
+    if(gen_is_antipodal(g, u[0], u[1]) || gen_is_antipodal(g, v[0], v[1])) return false;
+    if(gen_same_orbit(g, u[0], u[1], v[0], v[1])) return false;
+    t[0] = gen_rel(g, u[1], u[0]); t[1] = gen_rel(g, u[0], u[1]);
+    t[2] = gen_rel(g, v[1], v[0]); t[3] = gen_rel(g, v[0], v[1]);
+  }
+  gen_put(g, u[0], us[0], t[0]);
+  gen_put(g, u[1], us[1], t[1]);
+  gen_put(g, v[0], vs[0], t[2]);
+  gen_put(g, v[1], vs[1], t[3]);
+  return true;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Grid graphs: vertex v = x*h + y; symmetric grids store the base block.    */
+/* ------------------------------------------------------------------------ */
+
+static inline int gx(int v, int h) { return v / h; }
+static inline int gy(int v, int h) { return v % h; }
+
+/* ODP_ROTATE (utils.c:67-88) for s = 2 (180 degrees) and s = 4 (90/180/270, w == h). */
+static inline int grid_rot(const grid_ctx *g, int v, int deg)
+{
+  int x = gx(v, g->h), y = gy(v, g->h), h = g->h;
+  if(g->s == 2) return (g->w - x - 1) * h + (h - y - 1);
+  if(deg == 90)  return y * h + (h - x - 1);
+  if(deg == 180) return (h - x - 1) * h + (h - y - 1);
+  return (h - y - 1) * h + x;
+}
+
+/* Row of a base-block vertex (ODP_LOCAL_INDEX_GRID, utils.c:189-211). */
+static inline int grid_row(const grid_ctx *g, int v)
+{
+  if(g->s != 4) return v;
+  return gx(v, g->h) * g->bh + gy(v, g->h);
+}
+
+/* adjacency[v][j] of the expanded grid (GLOBAL_ADJ_GRID, utils.c:214-247). */
+static inline int grid_nbr(const grid_ctx *g, int v, int j)
+{
+  const int d = g->d;
+  if(g->s == 1) return g->adj[(size_t)v * d + j];
+  int x = gx(v, g->h), y = gy(v, g->h);
+  if(g->s == 2){
+    if(x < g->bw) return g->adj[(size_t)v * d + j];
+    return grid_rot(g, g->adj[(size_t)grid_rot(g, v, 180) * d + j], 180);
+  }
+  if(x < g->bw && y < g->bh) return g->adj[(size_t)grid_row(g, v) * d + j];
+  if(x < g->bw)  return grid_rot(g, g->adj[(size_t)grid_row(g, grid_rot(g, v, 270)) * d + j], 90);
+  if(y >= g->bh) return grid_rot(g, g->adj[(size_t)grid_row(g, grid_rot(g, v, 180)) * d + j], 180);
+  return grid_rot(g, g->adj[(size_t)grid_row(g, grid_rot(g, v, 90)) * d + j], 270);
+}
+
+/* Base row that stores vertex v's orbit (global2local_vertex_grid, utils.c:392-423). */
+static inline int grid_orbit_row(const grid_ctx *g, int v)
+{
+  if(g->s == 1) return v;
+  int x = gx(v, g->h), y = gy(v, g->h);
+  if(g->s == 2) return (x < g->bw) ? v : grid_rot(g, v, 180);
+  if(x < g->bw && y < g->bh) return grid_row(g, v);
+  if(x < g->bw)  return grid_row(g, grid_rot(g, v, 270));
+  if(y >= g->bh) return grid_row(g, grid_rot(g, v, 180));
+  return grid_row(g, grid_rot(g, v, 90));
+}
+
+/* adjacency[v][slot] = u through the symmetry (set_adjacency, utils.c:425-459). */
+static void grid_put(grid_ctx *g, int v, int slot, int u)
+{
+  const int d = g->d;
+  if(g->s == 1){ g->adj[(size_t)v * d + slot] = u; return; }
+  int x = gx(v, g->h), y = gy(v, g->h);
+  if(g->s == 2){
+    if(x < g->bw) g->adj[(size_t)v * d + slot] = u;
+    else g->adj[(size_t)grid_rot(g, v, 180) * d + slot] = grid_rot(g, u, 180);
+    return;
+  }
+  if(x < g->bw && y < g->bh)
+    g->adj[(size_t)grid_row(g, v) * d + slot] = u;
+  else if(x < g->bw)
+    g->adj[(size_t)grid_row(g, grid_rot(g, v, 270)) * d + slot] = grid_rot(g, u, 270);
+  else if(y >= g->bh)
+    g->adj[(size_t)grid_row(g, grid_rot(g, v, 180)) * d + slot] = grid_rot(g, u, 180);
+  else
+    g->adj[(size_t)grid_row(g, grid_rot(g, v, 90)) * d + slot] = grid_rot(g, u, 90);
+}
+
+static inline int grid_deg(const grid_ctx *g, int v)
+{
+  return g->ndeg ? g->ndeg[grid_orbit_row(g, v)] : g->d;
+}
+
+static inline bool grid_short(const grid_ctx *g, int u, int v)      /* CHECK_LENGTH, utils.c:52-56 */
+{
+  if(g->xy)
+    return abs(g->xy[2 * u] - g->xy[2 * v]) + abs(g->xy[2 * u + 1] - g->xy[2 * v + 1]) <= g->len;
+  return abs(gx(u, g->h) - gx(v, g->h)) + abs(gy(u, g->h) - gy(v, g->h)) <= g->len;
+}
+
+static int *grid_coords(int w, int h)
+{
+  int *xy = malloc(sizeof(int) * 2 * (size_t)w * h);
+  for(int v = 0; v < w * h; v++){ xy[2 * v] = v / h; xy[2 * v + 1] = v % h; }
+  return xy;
+}
+
+static inline bool grid_is_antipodal(const grid_ctx *g, int u, int v)  /* IS_DIAMETER_GRID, utils.c:104-110 */
+{
+  return g->s != 1 && u == grid_rot(g, v, 180);
+}
+
+/* get_degree_index_grid, utils.c:534-557 */
+static int grid_back_slot(const grid_ctx *g, int u, int v, int u_slot)
+{
+  if(u == v){
+    int dd = grid_deg(g, v);
+    for(int i = 0; i < dd; i++)
+      if(grid_nbr(g, v, i) == u && i != u_slot) return i;
+  }
+  else if(g->s != 1 && u == grid_rot(g, v, 180)){
+    return u_slot;
+  }
+  else{
+    int dd = grid_deg(g, v);
+    for(int i = 0; i < dd; i++)
+      if(grid_nbr(g, v, i) == u) return i;
+  }
+  ODP_FAIL("Something Wrong ! [id=5]\n");
+}
+
+/* check_rotated_edges_overlap_grid, utils.c:766-782 */
+static bool grid_same_orbit(const grid_ctx *g, int u0, int v0, int u1, int v1)
+{
+  if(g->s == 2)
+    return (u0 == grid_rot(g, u1, 180) && v0 == grid_rot(g, v1, 180)) ||
+           (u0 == grid_rot(g, v1, 180) && v0 == grid_rot(g, u1, 180));
+  if(g->s == 4){
+    for(int deg = 90; deg <= 270; deg += 90)
+      if(u0 == grid_rot(g, u1, deg) && v0 == grid_rot(g, v1, deg)) return true;
+    for(int deg = 90; deg <= 270; deg += 90)
+      if(u0 == grid_rot(g, v1, deg) && v0 == grid_rot(g, u1, deg)) return true;
+  }
+  return false;
+}
+
+/* mutate_adjacency_1opt_grid_s, utils.c:790-822 */
+static bool grid_one_opt(odp_rng *rng, grid_ctx *g, int u, int us)
+{
+  int s = g->s;
+  int v = grid_nbr(g, u, us);
+  if(grid_is_antipodal(g, u, v)) return false;
+  if(s == 2 && u == grid_rot(g, v, 180)) return false;
+  if(s == 4 && (u == grid_rot(g, v, 90) || u == grid_rot(g, v, 270))) return false;
+  int vs = grid_back_slot(g, u, v, us);
+  int k = odp_rng_below(rng, s);
+  if(k != s - 1){
+    int nv = grid_rot(g, v, (k + 1) * (360 / s));
+    int nu = grid_rot(g, u, (s - k - 1) * (360 / s));
+    if(!grid_short(g, u, nv)) return false;
+    grid_put(g, nv, vs, u);
+    grid_put(g, nu, us, v);
+  }
+  else{
+    int nv = grid_rot(g, u, 180);
+    int nu = grid_rot(g, v, 180);
+    if(!grid_short(g, u, nv) || !grid_short(g, v, nu)) return false;
+    grid_put(g, nv, us, u);
+    grid_put(g, nu, vs, v);
+  }
+  return true;
+}
+
+/* One 2-opt attempt on a grid(_s) graph (mutate_adjacency_2opt_grid_s, utils.c:824-971). */
+static bool grid_two_opt(odp_rng *rng, grid_ctx *g, ODP_Restore *r)
+{
+  int u[2], v[2], us[2], vs[2];
+  const int n = g->n;
+  for(;;){
+    u[0] = odp_rng_below(rng, n);
+    u[1] = odp_rng_below(rng, n);
+    if(u[0] == u[1]) continue;
+    us[0] = odp_rng_below(rng, grid_deg(g, u[0]));
+    v[0] = grid_nbr(g, u[0], us[0]);
+    if(v[0] == u[1]) continue;
+    us[1] = odp_rng_below(rng, grid_deg(g, u[1]));
+    v[1] = grid_nbr(g, u[1], us[1]);
+    if(v[1] == u[0] || v[0] == v[1]) continue;
+    break;
+  }
+  /* Reverse slots are resolved lazily (see file header): vs_ready tracks it. */
+  bool vs_ready = false;
+#define RESOLVE_BACK_SLOTS() do{ if(!vs_ready){ \
+    vs[0] = grid_back_slot(g, u[0], v[0], us[0]); \
+    vs[1] = grid_back_slot(g, u[1], v[1], us[1]); \
+    fill_restore(r, u, us, v, vs); vs_ready = true; } }while(0)
+
+  bool a0 = grid_is_antipodal(g, u[0], v[0]), a1 = grid_is_antipodal(g, u[1], v[1]);
+  if(a0 && a1){
+    if(g->s == 4 && (u[0] == grid_rot(g, u[1], 90) || u[0] == grid_rot(g, u[1], 270))) return false;
+    int t0, t1;
+    if(odp_rng_below(rng, 2)){ if(!grid_short(g, u[0], u[1])) return false; t0 = u[1]; t1 = u[0]; }
+    else                     { if(!grid_short(g, u[0], v[1])) return false; t0 = v[1]; t1 = v[0]; }
+    RESOLVE_BACK_SLOTS();
+    grid_put(g, u[0], us[0], t0);
+    grid_put(g, u[1], us[1], t1);
+    return true;
+  }
+  if(a0 || a1){
+    RESOLVE_BACK_SLOTS();       /* the restore record keeps the unswapped order */
+    if(a1){
+      int t;
+      t = u[0]; u[0] = u[1]; u[1] = t;
+      t = us[0]; us[0] = us[1]; us[1] = t;
+      t = v[0]; v[0] = v[1]; v[1] = t;
+      t = vs[0]; vs[0] = vs[1]; vs[1] = t;
+    }
+    int k = odp_rng_below(rng, 4), t[4];
+    int u1o = grid_rot(g, u[1], 180), v1o = grid_rot(g, v[1], 180);
+    switch(k){
+    case 0:
+      if(!grid_short(g, u[0], v[1]) || !grid_short(g, u[1], u1o)) return false;
+      t[0] = v[1]; t[1] = u1o; t[2] = v1o; t[3] = u[0];
+      break;
+    case 1:
+      if(!grid_short(g, u[0], v1o) || !grid_short(g, u[1], u1o)) return false;
+      t[0] = v1o; t[1] = u1o; t[2] = v[1]; t[3] = v[0];
+      break;
+    case 2:
+      if(!grid_short(g, u[0], u[1]) || !grid_short(g, v[1], v1o)) return false;
+      t[0] = u[1]; t[1] = u[0]; t[2] = u1o; t[3] = v1o;
+      break;
+    default:
+      if(!grid_short(g, u[0], u1o) || !grid_short(g, v[1], v1o)) return false;
+      t[0] = u1o; t[1] = v[0]; t[2] = u[1]; t[3] = v1o;
+      break;
+    }
+    grid_put(g, u[0], us[0], t[0]);
+    grid_put(g, u[1], us[1], t[1]);
+    grid_put(g, v[0], vs[0], t[2]);
+    grid_put(g, v[1], vs[1], t[3]);
+    return true;
+  }
+
+  if(grid_same_orbit(g, u[0], v[0], u[1], v[1])){
+    RESOLVE_BACK_SLOTS();
+    return grid_one_opt(rng, g, u[0], us[0]);
+  }
+
+  int t[4];
+  int cross = odp_rng_below(rng, 2);
+  {
+    /* Length test first and without a data-dependent branch: almost every
+     * proposal on a large grid fails here. */
+    int pu = cross ? v[1] : u[1], pv = cross ? u[1] : v[1];
+    if(!(grid_short(g, u[0], pu) & grid_short(g, v[0], pv))) return false;
+  }
+  if(cross){                            /* u0--v1, v0--u1 */
+    if(grid_is_antipodal(g, u[0], v[1]) || grid_is_antipodal(g, v[0], u[1])) return false;
+    if(grid_same_orbit(g, u[0], v[1], v[0], u[1])) return false;
+    t[0] = v[1]; t[1] = v[0]; t[2] = u[1]; t[3] = u[0];
+  }
+  else{                                 /* u0--u1, v0--v1 */
+    if(grid_is_antipodal(g, u[0], u[1]) || grid_is_antipodal(g, v[0], v[1])) return false;
+    if(grid_same_orbit(g, u[0], u[1], v[0], v[1])) return false;
+    t[0] = u[1]; t[1] = u[0]; t[2] = v[1]; t[3] = v[0];
+  }
+  RESOLVE_BACK_SLOTS();
+  grid_put(g, u[0], us[0], t[0]);
+  grid_put(g, u[1], us[1], t[1]);
+  grid_put(g, v[0], vs[0], t[2]);
+  grid_put(g, v[1], vs[1], t[3]);
+  return true;
+#undef RESOLVE_BACK_SLOTS
+}
+
+/* ------------------------------------------------------------------------ */
+/* Connectivity probe used by the generators (simple_bfs, utils.c:273-353).  */
+/* ------------------------------------------------------------------------ */
+
+static bool has_unreached_general(const gen_ctx *g)
+{
+  int n = g->n;
+  char *seen = calloc((size_t)n, 1);
+  int *queue = malloc(sizeof(int) * (size_t)n);
+  int head = 0, tail = 0;
+  queue[tail++] = 0; seen[0] = 1;
+  while(head < tail){
+    int v = queue[head++];
+    int p = v / g->base, m = v - p * g->base;
+    for(int j = 0; j < g->d; j++){
+      int x = g->adj[(size_t)m * g->d + j] + p * g->base;
+      if(x >= n) x -= n;
+      if(!seen[x]){ seen[x] = 1; queue[tail++] = x; }
+    }
+  }
+  free(queue); free(seen);
+  return tail != n;
+}
+
+static bool has_unreached_grid(const grid_ctx *g)
+{
+  int n = g->n;
+  char *seen = calloc((size_t)n, 1);
+  int *queue = malloc(sizeof(int) * (size_t)n);
+  int head = 0, tail = 0;
+  queue[tail++] = 0; seen[0] = 1;
+  while(head < tail){
+    int v = queue[head++];
+    for(int j = 0; j < g->d; j++){
+      int x = grid_nbr(g, v, j);
+      if(!seen[x]){ seen[x] = 1; queue[tail++] = x; }
+    }
+  }
+  free(queue); free(seen);
+  return tail != n;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Conversions.                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* ODP_Conv_edge2adjacency_general_s, utils.c:1012-1034 */
+static void edges_to_rows_general(int n, int lines, int d, const int (*edge)[2], int s, int *adj)
+{
+  int base = n / s;
+  int *cnt = calloc((size_t)base, sizeof(int));
+  for(size_t i = 0; i < (size_t)base * d; i++) adj[i] = UNSET;
+  for(int i = 0; i < lines; i++){
+    int a = edge[i][0], b = edge[i][1];
+    if(a < base) adj[(size_t)a * d + cnt[a]++] = b;
+    if(b < base) adj[(size_t)b * d + cnt[b]++] = a;
+  }
+  free(cnt);
+}
+
+/* ODP_Conv_edge2adjacency_grid_s, utils.c:1116-1151 (s = 2 or 4) */
+static void edges_to_rows_grid(int w, int h, int lines, int d, const int (*edge)[2], int s, int *adj)
+{
+  grid_ctx g = { .w = w, .h = h, .d = d, .s = s, .n = w * h, .bw = w / 2, .bh = (s == 2) ? h : h / 2 };
+  int base = g.n / s;
+  int *cnt = calloc((size_t)base, sizeof(int));
+  for(size_t i = 0; i < (size_t)base * d; i++) adj[i] = UNSET;
+  for(int i = 0; i < lines; i++){
+    int a = edge[i][0], b = edge[i][1];
+    if(gx(a, h) < g.bw && gy(a, h) < g.bh){ int r = grid_row(&g, a); adj[(size_t)r * d + cnt[r]++] = b; }
+    if(gx(b, h) < g.bw && gy(b, h) < g.bh){ int r = grid_row(&g, b); adj[(size_t)r * d + cnt[r]++] = a; }
+  }
+  free(cnt);
+}
+
+static int expected_lines(int n, int d, const int *ndeg)
+{
+  if(!ndeg) return (n * d) / 2;
+  long total = 0;
+  for(int i = 0; i < n; i++) total += ndeg[i];
+  if(total % 2 == 1) ODP_FAIL("Something Wrong ! [id=2]\n");
+  return (int)(total / 2);
+}
+
+/* ODP_Conv_adjacency2edge_general, utils.c:1506-1533 */
+static void rows_to_edges_full(int n, int d, const int *ndeg, const int *adj, int (*edge)[2])
+{
+  int lines = 0, loops = 0;
+  for(int i = 0; i < n; i++){
+    int dd = ndeg ? ndeg[i] : d;
+    for(int j = 0; j < dd; j++){
+      int v = adj[(size_t)i * d + j];
+      if(i < v){ edge[lines][0] = i; edge[lines][1] = v; lines++; }
+      else if(i == v){
+        loops++;
+        if(loops % 2 == 0){ edge[lines][0] = i; edge[lines][1] = v; lines++; }
+      }
+    }
+  }
+  if(loops % 2 == 1 || lines != expected_lines(n, d, ndeg))
+    ODP_FAIL("Something Wrong ! [id=1]\n");
+}
+
+/* ODP_Conv_adjacency2edge_general_s, utils.c:991-1010 */
+static void rows_to_edges_general(int n, int d, const int *ndeg, const int *adj, int s, int (*edge)[2])
+{
+  int base = n / s;
+  int *full = malloc(sizeof(int) * (size_t)n * d);
+  int *full_deg = ndeg ? malloc(sizeof(int) * (size_t)n) : NULL;
+  for(int i = 0; i < s; i++)
+    for(int j = 0; j < base; j++){
+      int dd = ndeg ? ndeg[j] : d;
+      if(full_deg) full_deg[i * base + j] = dd;
+      for(int k = 0; k < dd; k++)
+        full[(size_t)(i * base + j) * d + k] = wrap(adj[(size_t)j * d + k] + i * base, n);
+    }
+  /* The reference passes the base-sized num_degrees on to the n-row
+   * conversion (utils.c:1009); the per-row degrees are tiled here instead. */
+  rows_to_edges_full(n, d, full_deg, full, edge);
+  free(full_deg);
+  free(full);
+}
+
+/* ODP_Conv_adjacency2edge_grid_s, utils.c:152-169 / 154-168 */
+static void rows_to_edges_grid(int w, int h, int d, const int *ndeg, const int *adj, int s, int (*edge)[2])
+{
+  int n = w * h;
+  if(s == 1){ rows_to_edges_full(n, d, ndeg, adj, edge); return; }
+  grid_ctx g = { .w = w, .h = h, .d = d, .s = s, .n = n, .bw = w / 2, .bh = (s == 2) ? h : h / 2 };
+  int *full = malloc(sizeof(int) * (size_t)n * d);
+  int *full_deg = ndeg ? malloc(sizeof(int) * (size_t)n) : NULL;
+  int base = n / s;
+  for(int i = 0; i < base; i++){
+    int dd = ndeg ? ndeg[i] : d;
+    if(s == 2){
+      if(full_deg){ full_deg[i] = dd; full_deg[grid_rot(&g, i, 180)] = dd; }
+      for(int k = 0; k < dd; k++){
+        int v = adj[(size_t)i * d + k];
+        full[(size_t)i * d + k] = v;
+        full[(size_t)grid_rot(&g, i, 180) * d + k] = grid_rot(&g, v, 180);
+      }
+    }
+    else{
+      int j = (i / g.bh) * h + (i % g.bh);
+      if(full_deg){
+        full_deg[j] = dd;
+        for(int r = 90; r <= 270; r += 90) full_deg[grid_rot(&g, j, r)] = dd;
+      }
+      for(int k = 0; k < dd; k++){
+        int v = adj[(size_t)i * d + k];
+        full[(size_t)j * d + k] = v;
+        full[(size_t)grid_rot(&g, j, 90) * d + k]  = grid_rot(&g, v, 90);
+        full[(size_t)grid_rot(&g, j, 180) * d + k] = grid_rot(&g, v, 180);
+        full[(size_t)grid_rot(&g, j, 270) * d + k] = grid_rot(&g, v, 270);
+      }
+    }
+  }
+  rows_to_edges_full(n, d, full_deg, full, edge);
+  free(full_deg);
+  free(full);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Generators.                                                               */
+/* ------------------------------------------------------------------------ */
+
+static void check_nd(int n, int d)                    /* CHECK_PARAMETERS, utils.c:355-359 */
+{
+  if(n % 2 == 1 && d % 2 == 1)
+    ODP_FAIL("Nodes(%d) or Degree(%d) must be a multiple of 2.\n", n, d);
+}
+
+static void check_sym(int n, int s)
+{
+  if(s <= 0 || n % s != 0) ODP_FAIL("nodes(%d) must be divisible by symmetries(%d)\n", n, s);
+}
+
+static void check_grid_sym(int w, int h, int s)
+{
+  if(s != 1 && s != 2 && s != 4) ODP_FAIL("symmetries(%d) must be 1 or 2 or 4\n", s);
+  if(s == 2 && w % 2 != 0) ODP_FAIL("width(%d) must be divisible by 2\n", w);
+  else if(s == 4 && (w % 2 != 0 || h % 2 != 0)) ODP_FAIL("width(%d) and height(%d) must be divisible by 2\n", w, h);
+  else if(s == 4 && w != h) ODP_FAIL("Must be the same as width(%d) and height(%d)\n", w, h);
+}
+
+/* Ring with d/2 parallel edges per consecutive pair, plus antipodal chords
+ * when d is odd (create_simple_graph, utils.c:1041-1063). */
+static void ring_multigraph(int n, int d, int (*edge)[2])
+{
+  int hd = d / 2;
+  for(int i = 0; i < n - 1; i++)
+    for(int j = 0; j < hd; j++){ edge[i * hd + j][0] = i; edge[i * hd + j][1] = i + 1; }
+  for(int j = 0; j < hd; j++){ edge[(n - 1) * hd + j][0] = n - 1; edge[(n - 1) * hd + j][1] = 0; }
+  if(d % 2 == 1){
+    int half = n / 2;
+    for(int i = 0; i < half; i++){ edge[hd * n + i][0] = i; edge[hd * n + i][1] = i + half; }
+  }
+}
+
+/* ODP_Generate_random_general(_s), utils.c:1065-1114 */
+void odpx_generate_general(odp_rng *rng, int n, int d, int s, int (*edge)[2])
+{
+  check_sym(n, s);
+  check_nd(n, d);
+  ring_multigraph(n, d, edge);
+  int lines = (n * d) / 2;
+  gen_ctx g = { .n = n, .d = d, .s = s, .base = n / s, .ndeg = NULL };
+  g.adj = malloc(sizeof(int) * (size_t)g.base * d);
+  edges_to_rows_general(n, lines, d, (const int (*)[2])edge, s, g.adj);
+  for(long i = 0; i < (long)lines * GEN_ITERS; i++)
+    while(!gen_two_opt(rng, &g, NULL)) {}
+  while(has_unreached_general(&g))
+    while(!gen_two_opt(rng, &g, NULL)) {}
+  if(s == 1) rows_to_edges_full(n, d, NULL, g.adj, edge);
+  else       rows_to_edges_general(n, d, NULL, g.adj, s, edge);
+  free(g.adj);
+}
+
+static void grid_mutate_until(odp_rng *rng, grid_ctx *g, ODP_Restore *r)
+{
+  while(!grid_two_opt(rng, g, r)) {}
+}
+
+/* ODP_Generate_random_grid, utils.c:1577-1625 */
+static void generate_grid_plain(odp_rng *rng, int w, int h, int d, int len, int (*edge)[2])
+{
+  int n = w * h;
+  check_nd(n, d);
+  int i = 0;
+  for(int x = 0; x < w / 2; x++)
+    for(int y = 0; y < h; y++)
+      for(int k = 0; k < d; k++){
+        edge[i][0] = y + 2 * x * h;
+        edge[i][1] = edge[i][0] + h;
+        i++;
+      }
+  if(w % 2 == 1){
+    for(int y = 0; y < h / 2; y++)
+      for(int k = 0; k < d; k++){
+        edge[i][0] = (w - 1) * h + 2 * y;
+        edge[i][1] = edge[i][0] + 1;
+        i++;
+      }
+    if(h % 2 == 1)
+      for(int k = 0; k < d / 2; k++){ edge[i][0] = edge[i][1] = n - 1; i++; }
+  }
+  int lines = (n * d) / 2;
+  int *xy = grid_coords(w, h);
+  grid_ctx g = { .w = w, .h = h, .d = d, .s = 1, .len = len, .n = n, .bw = w / 2, .bh = h / 2, .ndeg = NULL, .xy = xy };
+  g.adj = malloc(sizeof(int) * (size_t)n * d);
+  edges_to_rows_general(n, lines, d, (const int (*)[2])edge, 1, g.adj);
+  for(long it = 0; it < (long)lines * GEN_ITERS; it++) grid_mutate_until(rng, &g, NULL);
+  gen_ctx probe = { .n = n, .d = d, .s = 1, .base = n, .adj = g.adj };
+  while(has_unreached_general(&probe)) grid_mutate_until(rng, &g, NULL);
+  rows_to_edges_full(n, d, NULL, g.adj, edge);
+  free(g.adj);
+  free(xy);
+}
+
+/* ODP_Generate_random_grid_s, utils.c:1627-1749 */
+void odpx_generate_grid(odp_rng *rng, int w, int h, int d, int len, int s, int (*edge)[2])
+{
+  check_nd(w * h, d);
+  check_grid_sym(w, h, s);
+  if(s == 1){ generate_grid_plain(rng, w, h, d, len, edge); return; }
+
+  grid_ctx g = { .w = w, .h = h, .d = d, .s = s, .len = len, .n = w * h, .bw = w / 2, .bh = (s == 2) ? h : h / 2 };
+  int n = g.n, lines = (n * d) / 2, base_lines = lines / s, base = n / s;
+  int bw = g.bw, bh = g.bh;
+  int deg_base = (base % 2 == 0 || d % 2 == 0) ? d : d - 1;
+  generate_grid_plain(rng, bw, bh, deg_base, len, edge);
+  int made = (deg_base == d) ? base_lines : (base * (d - 1)) / 2;
+  for(int i = 0; i < made; i++)
+    for(int j = 0; j < 2; j++)
+      edge[i][j] = gx(edge[i][j], bh) * h + gy(edge[i][j], bh);
+  if(s == 2){
+    for(int i = 0; i < made; i++)
+      for(int j = 0; j < 2; j++) edge[made + i][j] = grid_rot(&g, edge[i][j], 180);
+  }
+  else{
+    for(int i = 0; i < made; i++)
+      for(int j = 0; j < 2; j++){
+        edge[made + i][j]     = grid_rot(&g, edge[i][j], 90);
+        edge[made * 2 + i][j] = grid_rot(&g, edge[i][j], 180);
+        edge[made * 3 + i][j] = grid_rot(&g, edge[i][j], 270);
+      }
+  }
+  if(deg_base != d){                      /* odd base and odd degree: add a perfect matching */
+    int k = made * s;
+    if(s == 2){
+      for(int x = 0; x < w; x += 2)
+        for(int y = 0; y < h; y++){ edge[k][0] = y + x * h; edge[k][1] = edge[k][0] + h; k++; }
+    }
+    else{
+      for(int x = 0; x < bw / 2; x++)
+        for(int y = 0; y < bh; y++){
+          edge[k][0] = x * 2 * h + y;
+          edge[k][1] = edge[k][0] + h;
+          for(int r = 1; r < 4; r++){
+            edge[k + r][0] = grid_rot(&g, edge[k][0], 90 * r);
+            edge[k + r][1] = grid_rot(&g, edge[k][1], 90 * r);
+          }
+          k += 4;
+        }
+      if(bw % 2 == 1){
+        for(int y = 0; y < bh / 2; y++){
+          edge[k][0] = (bw - 1) * h + y * 2;
+          edge[k][1] = edge[k][0] + 1;
+          for(int r = 1; r < 4; r++){
+            edge[k + r][0] = grid_rot(&g, edge[k][0], 90 * r);
+            edge[k + r][1] = grid_rot(&g, edge[k][1], 90 * r);
+          }
+          k += 4;
+        }
+        if(bh % 2 == 1){
+          if(len <= 1) ODP_FAIL("Graphs with odd width/2 and length/2 and length 1 cannot be created.");
+          edge[k][0]     = (bw - 1) * h + (bh - 1);
+          edge[k][1]     = bw * h + bh;
+          edge[k + 1][0] = (bw - 1) * h + bh;
+          edge[k + 1][1] = bw * h + (bh - 1);
+        }
+      }
+    }
+  }
+  int *xy = grid_coords(w, h);
+  g.xy = xy;
+  g.adj = malloc(sizeof(int) * (size_t)base * d);
+  edges_to_rows_grid(w, h, lines, d, (const int (*)[2])edge, s, g.adj);
+  for(long it = 0; it < (long)base_lines * GEN_ITERS; it++) grid_mutate_until(rng, &g, NULL);
+  while(has_unreached_grid(&g)) grid_mutate_until(rng, &g, NULL);
+  rows_to_edges_grid(w, h, d, NULL, g.adj, s, edge);
+  free(g.adj);
+  free(xy);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Public odp.h utility surface.                                             */
+/* ------------------------------------------------------------------------ */
+
+static odp_rng g_libc_rng = { .libc = 1 };
+
+/* Parameters of the last Mutate call, which Restore reuses
+ * (the reference keeps the same file-scope state, utils.c:2). */
+static int m_nodes, m_degree, m_width, m_height, m_symmetries;
+
+void ODP_Srand(unsigned int seed) { srand(seed); }
+
+void ODP_Generate_random_general(int nodes, int degree, int (*edge)[2])
+{
+  odpx_generate_general(&g_libc_rng, nodes, degree, 1, edge);
+}
+
+void ODP_Generate_random_general_s(int nodes, int degree, int symmetries, int (*edge)[2])
+{
+  odpx_generate_general(&g_libc_rng, nodes, degree, symmetries, edge);
+}
+
+void ODP_Generate_random_grid(int width, int height, int degree, int length, int (*edge)[2])
+{
+  odpx_generate_grid(&g_libc_rng, width, height, degree, length, 1, edge);
+}
+
+void ODP_Generate_random_grid_s(int width, int height, int degree, int length, int symmetries, int (*edge)[2])
+{
+  odpx_generate_grid(&g_libc_rng, width, height, degree, length, symmetries, edge);
+}
+
+void ODPX_Generate_random_general_seeded(unsigned int seed, int nodes, int degree, int symmetries, int (*edge)[2])
+{
+  odp_rng g; odp_rng_seed(&g, seed);
+  odpx_generate_general(&g, nodes, degree, symmetries, edge);
+}
+
+void ODPX_Generate_random_grid_seeded(unsigned int seed, int width, int height, int degree, int length,
+                                      int symmetries, int (*edge)[2])
+{
+  odp_rng g; odp_rng_seed(&g, seed);
+  odpx_generate_grid(&g, width, height, degree, length, symmetries, edge);
+}
+
+void ODP_Conv_edge2adjacency_general(int nodes, int lines, int degree, int (*edge)[2], void *adjacency)
+{
+  edges_to_rows_general(nodes, lines, degree, (const int (*)[2])edge, 1, adjacency);
+}
+
+void ODP_Conv_edge2adjacency_general_s(int nodes, int lines, int degree, int (*edge)[2], int symmetries, void *adjacency)
+{
+  check_sym(nodes, symmetries);
+  edges_to_rows_general(nodes, lines, degree, (const int (*)[2])edge, symmetries, adjacency);
+}
+
+void ODP_Conv_edge2adjacency_grid(int width, int height, int lines, int degree, int (*edge)[2], void *adjacency)
+{
+  edges_to_rows_general(width * height, lines, degree, (const int (*)[2])edge, 1, adjacency);
+}
+
+void ODP_Conv_edge2adjacency_grid_s(int width, int height, int lines, int degree, int (*edge)[2], int symmetries,
+                                    void *adjacency)
+{
+  check_grid_sym(width, height, symmetries);
+  if(symmetries == 1) edges_to_rows_general(width * height, lines, degree, (const int (*)[2])edge, 1, adjacency);
+  else edges_to_rows_grid(width, height, lines, degree, (const int (*)[2])edge, symmetries, adjacency);
+}
+
+void ODP_Conv_adjacency2edge_general(int nodes, int degree, int *num_degrees, void *adjacency, int (*edge)[2])
+{
+  rows_to_edges_full(nodes, degree, num_degrees, adjacency, edge);
+}
+
+void ODP_Conv_adjacency2edge_grid(int width, int height, int degree, int *num_degrees, void *adjacency, int (*edge)[2])
+{
+  rows_to_edges_full(width * height, degree, num_degrees, adjacency, edge);
+}
+
+void ODP_Conv_adjacency2edge_general_s(int nodes, int degree, int *num_degrees, void *adjacency, int symmetries,
+                                       int (*edge)[2])
+{
+  check_sym(nodes, symmetries);
+  rows_to_edges_general(nodes, degree, num_degrees, adjacency, symmetries, edge);
+}
+
+void ODP_Conv_adjacency2edge_grid_s(int width, int height, int degree, int *num_degrees, void *adjacency,
+                                    int symmetries, int (*edge)[2])
+{
+  check_grid_sym(width, height, symmetries);
+  rows_to_edges_grid(width, height, degree, num_degrees, adjacency, symmetries, edge);
+}
+
+/* ODP_Mutate_adjacency_general(_s), utils.c:752-788 */
+void odpx_mutate_general(odp_rng *rng, int nodes, int degree, const int *num_degrees, int symmetries,
+                         ODP_Restore *r, int *adjacency)
+{
+  check_sym(nodes, symmetries);
+  gen_ctx g = { .n = nodes, .d = degree, .s = symmetries, .base = nodes / symmetries,
+                .ndeg = num_degrees, .adj = adjacency };
+  while(!gen_two_opt(rng, &g, r)) {}
+}
+
+/* ODP_Mutate_adjacency_grid(_s), utils.c:973-989, 2105-2113 */
+void odpx_mutate_grid(odp_rng *rng, int width, int height, int degree, const int *num_degrees, int length,
+                      int symmetries, ODP_Restore *r, int *adjacency)
+{
+  check_nd(width * height, degree);
+  check_grid_sym(width, height, symmetries);
+  grid_ctx g = { .w = width, .h = height, .d = degree, .s = symmetries, .len = length, .n = width * height,
+                 .bw = width / 2, .bh = (symmetries == 2) ? height : height / 2,
+                 .ndeg = num_degrees, .adj = adjacency };
+  grid_mutate_until(rng, &g, r);
+}
+
+void ODP_Mutate_adjacency_general_s(int nodes, int degree, int *num_degrees, int symmetries, ODP_Restore *r,
+                                    int (*adjacency)[degree])
+{
+  m_nodes = nodes; m_degree = degree; m_symmetries = symmetries;
+  odpx_mutate_general(&g_libc_rng, nodes, degree, num_degrees, symmetries, r, (int *)adjacency);
+}
+
+void ODP_Mutate_adjacency_general(int nodes, int degree, int *num_degrees, ODP_Restore *r, int (*adjacency)[degree])
+{
+  ODP_Mutate_adjacency_general_s(nodes, degree, num_degrees, 1, r, adjacency);
+}
+
+void ODP_Mutate_adjacency_grid_s(int width, int height, int degree, int *num_degrees, int length, int symmetries,
+                                 ODP_Restore *r, int (*adjacency)[degree])
+{
+  m_width = width; m_height = height; m_degree = degree; m_symmetries = symmetries;
+  odpx_mutate_grid(&g_libc_rng, width, height, degree, num_degrees, length, symmetries, r, (int *)adjacency);
+}
+
+void ODP_Mutate_adjacency_grid(int width, int height, int degree, int *num_degrees, int length, ODP_Restore *r,
+                               int (*adjacency)[degree])
+{
+  /* The reference's grid Mutate leaves the Restore state untouched unless
+   * the _s variant is used (utils.c:2105-2113); it is set here as well so that
+   * Restore after a plain grid Mutate writes through the right shape. */
+  m_width = width; m_height = height; m_degree = degree; m_symmetries = 1;
+  odpx_mutate_grid(&g_libc_rng, width, height, degree, num_degrees, length, 1, r, (int *)adjacency);
+}
+
+/* ODP_Restore_adjacency_general, utils.c:500-507 */
+void odpx_restore_general(int nodes, int degree, int symmetries, ODP_Restore r, int *adjacency)
+{
+  gen_ctx g = { .n = nodes, .d = degree, .s = symmetries, .base = nodes / symmetries };
+  for(int i = 0; i < 2; i++){
+    adjacency[(size_t)(r.u[i] % g.base) * degree + r.u_d[i]] = gen_rel(&g, r.v[i], r.u[i]);
+    adjacency[(size_t)(r.v[i] % g.base) * degree + r.v_d[i]] = gen_rel(&g, r.u[i], r.v[i]);
+  }
+}
+
+/* ODP_Restore_adjacency_grid, utils.c:461-467 */
+void odpx_restore_grid(int width, int height, int degree, int symmetries, ODP_Restore r, int *adjacency)
+{
+  grid_ctx g = { .w = width, .h = height, .d = degree, .s = symmetries, .n = width * height,
+                 .bw = width / 2, .bh = (symmetries == 2) ? height : height / 2, .adj = adjacency };
+  for(int i = 0; i < 2; i++){
+    grid_put(&g, r.u[i], r.u_d[i], r.v[i]);
+    grid_put(&g, r.v[i], r.v_d[i], r.u[i]);
+  }
+}
+
+void ODP_Restore_adjacency_general(ODP_Restore r, void *adjacency)
+{
+  odpx_restore_general(m_nodes, m_degree, m_symmetries, r, adjacency);
+}
+
+void ODP_Restore_adjacency_grid(ODP_Restore r, void *adjacency)
+{
+  odpx_restore_grid(m_width, m_height, m_degree, m_symmetries, r, adjacency);
+}
+
+/* Thread-safe, explicitly parameterised mutate for callers that keep one
+ * stream per annealing chain (the serving workload). */
+void ODPX_Mutate_adjacency_general_s_rng(void *rng_state, int nodes, int degree, const int *num_degrees,
+                                         int symmetries, ODP_Restore *r, int *adjacency)
+{
+  odpx_mutate_general((odp_rng *)rng_state, nodes, degree, num_degrees, symmetries, r, adjacency);
+}
+
+size_t ODPX_Rng_size(void) { return sizeof(odp_rng); }
+
+void ODPX_Rng_seed(void *rng_state, unsigned int seed) { odp_rng_seed((odp_rng *)rng_state, seed); }
+
+int ODPX_Rng_next(void *rng_state) { return odp_rng_next((odp_rng *)rng_state); }

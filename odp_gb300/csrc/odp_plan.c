@@ -1,0 +1,461 @@
+/*
+ * odp_plan.c -- builds and runs execution plans (odp_plan.h) on the CUDA
+ * layer.  This is the host runtime of the library: it sizes column chunks so
+ * the live bitsets stay in L2, orders jobs, lays out device memory, and
+ * replays one CUDA graph per evaluation so a call costs one host->device
+ * copy, two kernels and one small device->host copy, with no host round trip
+ * per BFS level (the reference does one per level, aspl_cuda.cu:62-82).
+ *
+ * Result semantics follow the reference exactly (aspl_cuda.cu:84-85,
+ * 121-125, 256-260): the ordered sum is accumulated in 64-bit integers,
+ * ASPL = sum / ((double)n - 1) / n computed as sum / (((double)n-1)*n), the
+ * returned sum is (long)(sum / 2.0), the diameter is the largest level at
+ * which a chunk became complete, and a graph with unreachable pairs returns
+ * INT_MAX / LONG_MAX / DBL_MAX.
+ */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <limits.h>
+#include <float.h>
+#include "odp_plan.h"
+#include "odp_gb300.h"
+
+#define ALIGN_UP(x, a) ((((x) + (a) - 1) / (a)) * (a))
+
+static int g_device_ready = 0, g_sm_count = 0;
+
+int odp_device_ready(void)
+{
+  if(g_device_ready) return 0;
+  int e = gbx_device_init(&g_sm_count);
+  if(e) return e;
+  g_device_ready = 1;
+  return 0;
+}
+
+static int env_int(const char *name, int fallback)
+{
+  const char *v = getenv(name);
+  return (v && *v) ? atoi(v) : fallback;
+}
+
+void odp_tuning_defaults(odp_tuning *t, int batch)
+{
+  t->wc_log2 = env_int("ODP_GB300_WC_LOG2", 0);
+  t->slots = env_int("ODP_GB300_SLOTS", 0);
+  t->tile_rows = env_int("ODP_GB300_TILE_ROWS", 0);
+  t->l2_budget_mb = env_int("ODP_GB300_L2_MB", 80);
+  t->local_kb = env_int("ODP_GB300_LOCAL_KB", batch ? 2048 : 96);
+  t->use_graph = env_int("ODP_GB300_GRAPH", 1);
+  t->blocks = env_int("ODP_GB300_BLOCKS", 0);
+}
+
+static int ilog2_ceil(long long x)
+{
+  int l = 0;
+  while((1LL << l) < x) l++;
+  return l;
+}
+
+/* Rows one CTA pass covers for a chunk of 2^wl words (see RowShape in the .cu). */
+static int rows_per_pass(int wl)
+{
+  int vpr = (1 << wl) / 2;
+  int g = vpr < 32 ? vpr : 32;
+  return 8 * (32 / g);
+}
+
+static int validate_shape(const odp_shape *sh)
+{
+  int n = sh->grid ? sh->width * sh->height : sh->nodes;
+  if(n <= 0 || sh->degree < 0 || sh->symmetries <= 0) return ODPX_ERR_INVALID;
+  if(n % sh->symmetries != 0) return ODPX_ERR_INVALID;
+  if(sh->grid && sh->symmetries != 1){
+    int s = sh->symmetries, w = sh->width, h = sh->height;
+    if(s != 2 && s != 4) return ODPX_ERR_INVALID;
+    if(s == 2 && w % 2 != 0) return ODPX_ERR_INVALID;
+    if(s == 4 && (w % 2 != 0 || h % 2 != 0 || w != h)) return ODPX_ERR_INVALID;
+  }
+  return 0;
+}
+
+/* ODP_ROTATE (reference utils.c:67-88) on the host, for row tables. */
+static int rotate_host(int v, int width, int height, int s, int deg)
+{
+  int x = v / height, y = v % height;
+  if(s == 2) return (width - x - 1) * height + (height - y - 1);
+  if(deg == 90)  return y * height + (height - x - 1);
+  if(deg == 180) return (height - x - 1) * height + (height - y - 1);
+  return (height - y - 1) * height + x;
+}
+
+/* Vertex -> row table of a rotation-symmetric grid (ODP_Create_itable, utils.c:2103-2124). */
+static void fill_itable(int width, int height, int s, int *itable)
+{
+  int base = (width * height) / s;
+  if(s == 2){
+    for(int i = 0; i < base; i++){
+      itable[i] = i;
+      itable[rotate_host(i, width, height, s, 180)] = i + base;
+    }
+  }
+  else{
+    int bh = height / 2;
+    for(int i = 0; i < base; i++){
+      int v = (i / bh) * height + (i % bh);
+      itable[v] = i;
+      itable[rotate_host(v, width, height, s, 90)]  = i + base;
+      itable[rotate_host(v, width, height, s, 180)] = i + base * 2;
+      itable[rotate_host(v, width, height, s, 270)] = i + base * 3;
+    }
+  }
+}
+
+/* Per-vertex degrees over all n vertices, as the reference's Init variants
+ * expand them (aspl_cuda.cu:164-179 tiling, :200-217 rotation).  For s = 4
+ * grids the base vertex of local index i is placed with the inverse of the
+ * local index map, as the row table does. */
+static void fill_degrees(const odp_shape *sh, int n, int *out)
+{
+  int s = sh->symmetries, base = n / s;
+  const int *nd = sh->num_degrees;
+  if(!sh->grid || s == 1){
+    for(int t = 0; t < s; t++)
+      for(int j = 0; j < base; j++) out[t * base + j] = nd[j];
+    return;
+  }
+  int w = sh->width, h = sh->height;
+  if(s == 2){
+    for(int i = 0; i < base; i++){
+      out[i] = nd[i];
+      out[rotate_host(i, w, h, 2, 180)] = nd[i];
+    }
+  }
+  else{
+    for(int i = 0; i < base; i++){
+      int v = (i / (h / 2)) * h + i % (h / 2);
+      out[v] = nd[i];
+      out[rotate_host(v, w, h, 4, 90)]  = nd[i];
+      out[rotate_host(v, w, h, 4, 180)] = nd[i];
+      out[rotate_host(v, w, h, 4, 270)] = nd[i];
+    }
+  }
+}
+
+typedef struct { int job; double work; } job_order;
+
+static int cmp_work_desc(const void *a, const void *b)
+{
+  double wa = ((const job_order *)a)->work, wb = ((const job_order *)b)->work;
+  if(wa > wb) return -1;
+  if(wa < wb) return 1;
+  return ((const job_order *)a)->job - ((const job_order *)b)->job;
+}
+
+#define CK(call) do{ int _e = (call); if(_e){ rc = ODPX_ERR_CUDA; goto fail; } }while(0)
+
+int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning, odp_plan **out)
+{
+  int rc = 0;
+  *out = NULL;
+  if(count <= 0) return ODPX_ERR_INVALID;
+  if(odp_device_ready()) return ODPX_ERR_CUDA;
+  for(int i = 0; i < count; i++){
+    rc = validate_shape(&shapes[i]);
+    if(rc) return rc;
+  }
+
+  odp_plan *p = calloc(1, sizeof(odp_plan));
+  p->tuning = *tuning;
+  p->ngraphs = count;
+  p->g = calloc((size_t)count, sizeof(odp_plan_graph));
+  p->blocks = tuning->blocks > 0 ? tuning->blocks : gbx_engine_blocks();
+  p->spin_limit_ns = 60ull * 1000000000ull;
+  const double budget = (double)tuning->l2_budget_mb * 1024.0 * 1024.0;
+  const double local_bytes = (double)tuning->local_kb * 1024.0;
+
+  /* Shapes, chunk widths, tiles. */
+  int njobs = 0;
+  for(int i = 0; i < count; i++){
+    const odp_shape *sh = &shapes[i];
+    odp_plan_graph *g = &p->g[i];
+    g->grid = sh->grid;
+    g->n = sh->grid ? sh->width * sh->height : sh->nodes;
+    g->d = sh->degree;
+    g->dp = ALIGN_UP(sh->degree > 0 ? sh->degree : 1, 4);
+    g->s = sh->symmetries;
+    g->grid_s = sh->grid && sh->symmetries != 1;
+    g->width = sh->width;
+    g->height = sh->height;
+    g->B = g->n / g->s;
+    g->W = (g->B + 63) / 64;
+    int full_l2 = ilog2_ceil(g->W < 2 ? 2 : g->W);
+    int wl;
+    if(tuning->wc_log2 > 0) wl = tuning->wc_log2;
+    else if(count > 1) wl = full_l2 < 7 ? full_l2 : 7;          /* batch: whole rows up to 1 KB */
+    else{
+      /* single graph: widest chunk (<= 512 B rows) whose two buffers, for
+       * two concurrently active chunks, fit the L2 budget; very large n
+       * streams from HBM with 256 B rows */
+      wl = full_l2 < 6 ? full_l2 : 6;
+      while(wl > 3 && 2.0 * 2.0 * g->n * (double)(1 << wl) * 8.0 > budget) wl--;
+      if(2.0 * 2.0 * g->n * (double)(1 << wl) * 8.0 > budget) wl = full_l2 < 5 ? full_l2 : 5;
+    }
+    if(wl < 1) wl = 1;
+    if(wl > 8) wl = 8;
+    if(wl > full_l2 && full_l2 >= 1) wl = full_l2;
+    g->wc_log2 = wl;
+    const int wc = 1 << wl;
+    g->nchunks = (g->W + wc - 1) / wc;
+    double level_bytes = (double)g->n * wc * 8.0 * (g->d + 2);
+    int rpp = rows_per_pass(wl);
+    if(tuning->tile_rows > 0) g->tile_rows = tuning->tile_rows;
+    else if(level_bytes <= local_bytes) g->tile_rows = g->n;
+    else{
+      double per_row = (double)wc * 8.0 * (g->d + 2);
+      int tr = (int)(256.0 * 1024.0 / per_row);
+      g->tile_rows = ALIGN_UP(tr < rpp ? rpp : tr, rpp);
+    }
+    if(g->tile_rows > g->n) g->tile_rows = g->n;
+    if(g->tile_rows < 1) g->tile_rows = 1;
+    g->ntiles = (g->n + g->tile_rows - 1) / g->tile_rows;
+    g->has_ndeg = sh->num_degrees != NULL;
+    g->has_itable = g->grid_s;
+    g->adj_ints = (size_t)g->B * g->d;
+    g->adj_off = p->adj_ints;       p->adj_ints += ALIGN_UP(g->adj_ints, 4);
+    g->ndeg_off = p->ndeg_ints;     if(g->has_ndeg) p->ndeg_ints += ALIGN_UP((size_t)g->n, 4);
+    g->itable_off = p->itable_ints; if(g->has_itable) p->itable_ints += ALIGN_UP((size_t)g->n, 4);
+    g->nbr_off = p->nbr_ints;       p->nbr_ints += (size_t)g->n * g->dp;
+    p->total_vertices += g->n;
+    njobs += g->nchunks;
+  }
+  p->njobs = njobs;
+
+  /* Jobs, largest first so the long ones start early. */
+  gbx_job *jobs = calloc((size_t)njobs, sizeof(gbx_job));
+  job_order *ord = calloc((size_t)njobs, sizeof(job_order));
+  {
+    int k = 0;
+    for(int i = 0; i < count; i++){
+      odp_plan_graph *g = &p->g[i];
+      int wc = 1 << g->wc_log2;
+      for(int c = 0; c < g->nchunks; c++, k++){
+        gbx_job *j = &jobs[k];
+        j->n = g->n; j->dp = g->dp; j->wc_log2 = g->wc_log2;
+        j->src0 = c * wc * 64;
+        j->nsrc = g->B - j->src0 < wc * 64 ? g->B - j->src0 : wc * 64;
+        j->sym = g->s; j->graph = i;
+        j->tile_rows = g->tile_rows; j->ntiles = g->ntiles;
+        ord[k].job = k;
+        ord[k].work = (double)g->n * wc * (g->d + 2) * (count > 1 ? 1.0 : 0.0);
+      }
+    }
+  }
+  qsort(ord, (size_t)njobs, sizeof(job_order), cmp_work_desc);
+  p->h_jobs = calloc((size_t)njobs, sizeof(gbx_job));
+  for(int k = 0; k < njobs; k++) p->h_jobs[k] = jobs[ord[k].job];
+  free(jobs);
+  free(ord);
+
+  /* Slots: as many concurrent jobs as the L2 budget holds (at least 2 when
+   * there are 2 jobs), capped by the job count. */
+  size_t max_words = 0;
+  double sum_fp = 0;
+  int fit = 0;
+  for(int k = 0; k < njobs; k++){
+    size_t w = (size_t)p->h_jobs[k].n << p->h_jobs[k].wc_log2;
+    if(w > max_words) max_words = w;
+    double fp = 2.0 * 8.0 * (double)w;
+    if(sum_fp + fp <= budget){ sum_fp += fp; fit++; }
+  }
+  int nslots = tuning->slots > 0 ? tuning->slots : fit;
+  if(tuning->slots <= 0){
+    if(nslots < 2) nslots = 2;
+    if(count > 1 && nslots < 32) nslots = 32;
+    if(nslots > 512) nslots = 512;
+  }
+  if(nslots > njobs) nslots = njobs;
+  if(nslots < 1) nslots = 1;
+  p->nslots = nslots;
+  p->slot_words = ALIGN_UP(max_words, 32);
+
+  /* Device memory. */
+  p->out_off = sizeof(gbx_slot) * (size_t)nslots;
+  p->acc_off = p->out_off + sizeof(gbx_ctrl) + 64;
+  p->levels_off = p->acc_off + ALIGN_UP(sizeof(gbx_graph_acc) * (size_t)count, 64);
+  p->state_bytes = p->levels_off + ALIGN_UP(sizeof(int) * (size_t)njobs, 64);
+  p->out_bytes = p->state_bytes - p->out_off;
+
+  CK(gbx_stream_create(&p->stream));
+  CK(gbx_malloc((void **)&p->d_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4)));
+  if(p->ndeg_ints) CK(gbx_malloc((void **)&p->d_ndeg, sizeof(int) * p->ndeg_ints));
+  if(p->itable_ints) CK(gbx_malloc((void **)&p->d_itable, sizeof(int) * p->itable_ints));
+  CK(gbx_malloc((void **)&p->d_nbr, sizeof(int) * (p->nbr_ints ? p->nbr_ints : 4)));
+  CK(gbx_malloc((void **)&p->d_slotbuf, sizeof(unsigned long long) * p->slot_words * 2 * (size_t)nslots));
+  CK(gbx_malloc((void **)&p->d_expand, sizeof(gbx_expand_desc) * (size_t)count));
+  CK(gbx_malloc((void **)&p->d_jobs, sizeof(gbx_job) * (size_t)njobs));
+  CK(gbx_malloc((void **)&p->d_state, p->state_bytes));
+  CK(gbx_host_alloc((void **)&p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4)));
+  CK(gbx_host_alloc((void **)&p->h_state_init, p->state_bytes));
+  CK(gbx_host_alloc((void **)&p->h_state_out, p->out_bytes));
+
+  /* Static tables: degrees, row tables, expand descriptors, jobs. */
+  {
+    int *h_nd = p->ndeg_ints ? malloc(sizeof(int) * p->ndeg_ints) : NULL;
+    int *h_it = p->itable_ints ? malloc(sizeof(int) * p->itable_ints) : NULL;
+    gbx_expand_desc *ed = calloc((size_t)count, sizeof(gbx_expand_desc));
+    long long first = 0;
+    for(int i = 0; i < count; i++){
+      odp_plan_graph *g = &p->g[i];
+      if(g->has_ndeg) fill_degrees(&shapes[i], g->n, h_nd + g->ndeg_off);
+      if(g->has_itable) fill_itable(g->width, g->height, g->s, h_it + g->itable_off);
+      gbx_expand_desc *e = &ed[i];
+      e->adj = p->d_adj + g->adj_off;
+      e->ndeg = g->has_ndeg ? p->d_ndeg + g->ndeg_off : NULL;
+      e->itable = g->has_itable ? p->d_itable + g->itable_off : NULL;
+      e->nbr = p->d_nbr + g->nbr_off;
+      e->n = g->n; e->d = g->d; e->dp = g->dp; e->s = g->s;
+      e->width = g->width; e->height = g->height; e->grid_s = g->grid_s;
+      e->first_vertex = first;
+      first += g->n;
+    }
+    for(int k = 0; k < njobs; k++) p->h_jobs[k].nbr = p->d_nbr + p->g[p->h_jobs[k].graph].nbr_off;
+    if(h_nd) CK(gbx_memcpy_h2d(p->d_ndeg, h_nd, sizeof(int) * p->ndeg_ints, p->stream));
+    if(h_it) CK(gbx_memcpy_h2d(p->d_itable, h_it, sizeof(int) * p->itable_ints, p->stream));
+    CK(gbx_memcpy_h2d(p->d_expand, ed, sizeof(gbx_expand_desc) * (size_t)count, p->stream));
+    CK(gbx_memcpy_h2d(p->d_jobs, p->h_jobs, sizeof(gbx_job) * (size_t)njobs, p->stream));
+    CK(gbx_stream_sync(p->stream));
+    free(h_nd); free(h_it); free(ed);
+  }
+
+  /* Initial engine state: the first nslots jobs loaded into the slots. */
+  {
+    memset(p->h_state_init, 0, p->state_bytes);
+    gbx_slot *sl = (gbx_slot *)p->h_state_init;
+    for(int k = 0; k < nslots; k++){
+      const gbx_job *j = &p->h_jobs[k];
+      sl[k].ticket = (unsigned long long)j->ntiles << 32;
+      sl[k].job = k;
+      sl[k].level = 1;
+      sl[k].prev = (unsigned long long)j->nsrc;
+      sl[k].sum = ((long long)j->n * j->nsrc - j->nsrc) * j->sym;
+      sl[k].buf0 = p->d_slotbuf + (size_t)k * 2 * p->slot_words;
+      sl[k].buf1 = sl[k].buf0 + p->slot_words;
+    }
+    gbx_ctrl *ctrl = (gbx_ctrl *)(p->h_state_init + p->out_off);
+    ctrl->next_job = (unsigned)nslots;
+  }
+  *out = p;
+  return 0;
+
+fail:
+  odp_plan_destroy(p);
+  return rc;
+}
+
+void odp_plan_destroy(odp_plan *p)
+{
+  if(!p) return;
+  if(p->graph_exec) gbx_graph_destroy(p->graph_exec);
+  gbx_free(p->d_adj); gbx_free(p->d_ndeg); gbx_free(p->d_itable); gbx_free(p->d_nbr);
+  gbx_free(p->d_slotbuf); gbx_free(p->d_expand); gbx_free(p->d_jobs); gbx_free(p->d_state);
+  gbx_host_free(p->h_adj); gbx_host_free(p->h_state_init); gbx_host_free(p->h_state_out);
+  if(p->stream) gbx_stream_destroy(p->stream);
+  free(p->h_jobs);
+  free(p->g);
+  free(p);
+}
+
+/* The per-call GPU work, in stream order. */
+static int enqueue(odp_plan *p)
+{
+  int e;
+  if((e = gbx_memcpy_h2d(p->d_adj, p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4), p->stream))) return e;
+  if((e = gbx_memcpy_h2d(p->d_state, p->h_state_init, p->state_bytes, p->stream))) return e;
+  if((e = gbx_expand(p->d_expand, p->ngraphs, p->total_vertices,
+                     (unsigned int *)(p->d_state + p->out_off + sizeof(gbx_ctrl)), p->stream))) return e;
+  if((e = odp_plan_enqueue_engine(p))) return e;
+  return gbx_memcpy_d2h(p->h_state_out, p->d_state + p->out_off, p->out_bytes, p->stream);
+}
+
+int odp_plan_enqueue_engine(odp_plan *p)
+{
+  return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
+                           (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),
+                           (int *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->stream);
+}
+
+const int *odp_plan_job_levels(const odp_plan *p)
+{
+  return (const int *)(p->h_state_out + (p->levels_off - p->out_off));
+}
+
+void odp_plan_stage(odp_plan *p, const int *const *adjacency)
+{
+  for(int i = 0; i < p->ngraphs; i++){
+    const odp_plan_graph *g = &p->g[i];
+    memcpy(p->h_adj + g->adj_off, adjacency[i], sizeof(int) * g->adj_ints);
+  }
+}
+
+int odp_plan_launch(odp_plan *p)
+{
+  if(p->tuning.use_graph){
+    if(!p->graph_exec){
+      if(gbx_capture_begin(p->stream)) return ODPX_ERR_CUDA;
+      int e = enqueue(p);
+      void *ge = NULL;
+      int e2 = gbx_capture_end(p->stream, &ge);
+      if(e || e2) return ODPX_ERR_CUDA;
+      p->graph_exec = ge;
+    }
+    return gbx_graph_launch(p->graph_exec, p->stream) ? ODPX_ERR_CUDA : 0;
+  }
+  return enqueue(p) ? ODPX_ERR_CUDA : 0;
+}
+
+int odp_plan_finish(odp_plan *p, odp_result *results)
+{
+  if(gbx_stream_sync(p->stream)) return ODPX_ERR_CUDA;
+  const gbx_ctrl *ctrl = (const gbx_ctrl *)p->h_state_out;
+  unsigned int err = *(const unsigned int *)(p->h_state_out + sizeof(gbx_ctrl)) | ctrl->error;
+  if(err & GBX_ERR_TIMEOUT) return ODPX_ERR_TIMEOUT;
+  if(err & GBX_ERR_BAD_ADJ) return ODPX_ERR_ADJACENCY;
+  const gbx_graph_acc *acc = (const gbx_graph_acc *)(p->h_state_out + (p->acc_off - p->out_off));
+  p->bytes_alg_last = 0;
+  for(int i = 0; i < p->ngraphs; i++){
+    const odp_plan_graph *g = &p->g[i];
+    odp_result *r = &results[i];
+    if(acc[i].flags & 1){
+      r->diameter = INT_MAX;
+      r->sum = LONG_MAX;
+      r->aspl = DBL_MAX;
+      continue;
+    }
+    long sum = (long)acc[i].sum;
+    r->diameter = acc[i].levels;
+    r->aspl = sum / (((double)g->n - 1) * g->n);
+    r->sum = (long)(sum / 2.0);
+  }
+  return 0;
+}
+
+int odp_plan_run(odp_plan *p, const int *const *adjacency, odp_result *results)
+{
+  odp_plan_stage(p, adjacency);
+  int rc = odp_plan_launch(p);
+  if(rc) return rc;
+  return odp_plan_finish(p, results);
+}
+
+unsigned long long odp_plan_tiles(const odp_plan *p)
+{
+  return ((const gbx_ctrl *)p->h_state_out)->tiles;
+}
+
+unsigned int odp_plan_error(const odp_plan *p)
+{
+  const gbx_ctrl *ctrl = (const gbx_ctrl *)p->h_state_out;
+  return *(const unsigned int *)(p->h_state_out + sizeof(gbx_ctrl)) | ctrl->error;
+}

@@ -1,0 +1,36 @@
+"""The C-ABI library loads without a GPU and exports every entry point that
+include/*.h declares.  No compute calls (CPU only)."""
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_functions():
+    names = set()
+    for h in ("odp.h", "odp_gb300.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"^\s*(?:extern\s+)?[A-Za-z_][\w\s\*]*?\b((?:ODP|ODPX)_\w+)\s*\(", text, re.M):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_headers_declare_the_drop_in_surface():
+    names = declared_functions()
+    for n in ["ODP_Init_aspl_general", "ODP_Init_aspl_general_s", "ODP_Init_aspl_grid", "ODP_Init_aspl_grid_s",
+              "ODP_Set_aspl", "ODP_Finalize_aspl", "ODP_Set_aspl_batch"]:
+        assert n in names
+
+
+def test_library_exports_every_declared_symbol():
+    import odp_gb300
+    lib = ctypes.CDLL(odp_gb300.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_static_archive_built():
+    import odp_gb300.build as b
+    assert os.path.exists(b.A_PATH)

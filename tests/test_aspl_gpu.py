@@ -1,0 +1,280 @@
+"""GPU parity: the library's ASPL path (through its C ABI) against the
+reference's golden vectors and the oracle.  Every comparison is bit-exact:
+diameter and sum as integers, ASPL by its IEEE-754 bits."""
+import os
+import subprocess
+import sys
+import textwrap
+
+import numpy as np
+import pytest
+
+import odp_gb300 as og
+import oracle
+from conftest import (ROOT, case_adjacency, case_degrees, edges_to_adjacency, gen_record_adjacency, gen_record_edges,
+                      result_tuple, same, sha256)
+
+pytestmark = pytest.mark.gpu
+
+
+def gpu_aspl(adj, nodes=0, num_degrees=None, symmetries=1, grid=False, width=0, height=0):
+    """Init / Set / Finalize through the drop-in API."""
+    adj = np.ascontiguousarray(adj, dtype=np.int32)
+    d = adj.shape[1]
+    if grid:
+        if symmetries == 1:
+            og.init_aspl_grid(width, height, d, num_degrees)
+        else:
+            og.init_aspl_grid_s(width, height, d, num_degrees, symmetries)
+    else:
+        if symmetries == 1:
+            og.init_aspl_general(nodes, d, num_degrees)
+        else:
+            og.init_aspl_general_s(nodes, d, num_degrees, symmetries)
+    try:
+        return og.set_aspl(adj)
+    finally:
+        og.finalize_aspl()
+
+
+def test_sample_golden_tables(golden):
+    for s in golden["samples"]:
+        e = np.array(s["edges"], dtype=np.int32).reshape(-1, 2)
+        if "expected" in s:
+            if s["kind"] == "general":
+                n = int(e.max()) + 1
+                deg = int(np.bincount(e.reshape(-1), minlength=n).max())
+                got = gpu_aspl(og.conv_edge2adjacency_general(n, e, deg), nodes=n)
+            else:
+                n = s["width"] * s["height"]
+                deg = int(np.bincount(e.reshape(-1), minlength=n).max())
+                got = gpu_aspl(og.conv_edge2adjacency_grid(s["width"], s["height"], e, deg), grid=True,
+                               width=s["width"], height=s["height"])
+            exp = s["expected"]
+            assert (got[0], got[1], "%.10f" % got[2]) == (exp["diameter"], exp["sum"], exp["aspl"]), s["file"]
+        else:
+            if s["kind"] == "general":
+                adj = og.conv_edge2adjacency_general(s["nodes"], e, s["degree"], s["symmetries"])
+                got = gpu_aspl(adj, nodes=s["nodes"], symmetries=s["symmetries"])
+            else:
+                adj = og.conv_edge2adjacency_grid(s["width"], s["height"], e, s["degree"], s["symmetries"])
+                got = gpu_aspl(adj, grid=True, width=s["width"], height=s["height"], symmetries=s["symmetries"])
+            assert same(got, result_tuple(s["reference"])), s["file"]
+
+
+def test_edge_cases(golden):
+    for c in golden["cases"]:
+        adj = case_adjacency(c)
+        nd = case_degrees(c)
+        if c["kind"] == "general":
+            got = gpu_aspl(adj, nodes=c["nodes"], num_degrees=nd, symmetries=c["symmetries"])
+        else:
+            got = gpu_aspl(adj, grid=True, width=c["width"], height=c["height"], num_degrees=nd,
+                           symmetries=c["symmetries"])
+        assert same(got, result_tuple(c["reference"])), (c["name"], got, c["reference"])
+
+
+def test_generated_fixtures(golden):
+    for g in golden["generators"]:
+        if g.get("big"):
+            continue
+        e = gen_record_edges(og, g)
+        adj = gen_record_adjacency(og, g, e)
+        if g["kind"] == "general":
+            got = gpu_aspl(adj, nodes=g["nodes"], symmetries=g["symmetries"])
+        else:
+            got = gpu_aspl(adj, grid=True, width=g["width"], height=g["height"], symmetries=g["symmetries"])
+        assert same(got, result_tuple(g["reference"])), (g, got)
+
+
+def random_graph(rng):
+    """A random generated graph of random kind/shape, with its batch spec."""
+    if rng.random() < 0.7:
+        s = int(rng.choice([1, 1, 2, 4, 8]))
+        base = int(rng.integers(8, 400))
+        n = base * s
+        d = int(rng.integers(3, 12))
+        if n % 2 and d % 2:
+            d += 1
+        e = og.generate_random_general(n, d, s, seed=int(rng.integers(1 << 30)))
+        adj = og.conv_edge2adjacency_general(n, e, d, s)
+        return og.GraphSpec(adj, nodes=n, symmetries=s), dict(nodes=n, symmetries=s)
+    s = int(rng.choice([1, 2, 4]))
+    w = 2 * int(rng.integers(2, 9))
+    h = w if s == 4 else 2 * int(rng.integers(2, 9))
+    d = int(rng.integers(3, 7))
+    length = int(rng.integers(2, 5))
+    e = og.generate_random_grid(w, h, d, length, s, seed=int(rng.integers(1 << 30)))
+    adj = og.conv_edge2adjacency_grid(w, h, e, d, s)
+    return (og.GraphSpec(adj, grid=True, width=w, height=h, symmetries=s),
+            dict(grid=True, width=w, height=h, symmetries=s))
+
+
+def test_random_graphs_against_oracle():
+    rng = np.random.default_rng(123)
+    for _ in range(40):
+        spec, kw = random_graph(rng)
+        assert same(gpu_aspl(spec.adjacency, **kw), oracle.aspl(spec.adjacency, **kw)), kw
+
+
+def test_batch_matches_single_and_oracle(golden):
+    rng = np.random.default_rng(5)
+    specs, kws = [], []
+    for _ in range(60):
+        spec, kw = random_graph(rng)
+        specs.append(spec)
+        kws.append(kw)
+    for c in golden["cases"]:        # non-regular, directed, disconnected, tiny graphs
+        if c["kind"] == "general":
+            specs.append(og.GraphSpec(case_adjacency(c), nodes=c["nodes"], symmetries=c["symmetries"],
+                                      num_degrees=case_degrees(c)))
+            kws.append(dict(nodes=c["nodes"], symmetries=c["symmetries"], num_degrees=case_degrees(c)))
+    got = og.set_aspl_batch(specs)
+    for spec, kw, g in zip(specs, kws, got):
+        assert same(g, oracle.aspl(spec.adjacency, **kw)), kw
+    # the cached plan is reused on a second call with new adjacency
+    got2 = og.set_aspl_batch(specs)
+    assert all(same(a, b) for a, b in zip(got, got2))
+
+
+def test_batch_plan_reuse_with_new_adjacency():
+    n, d = 512, 6
+    adjs = [og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=s), d) for s in range(8)]
+    b = og.Batch([og.GraphSpec(a, nodes=n) for a in adjs])
+    first = b.run()
+    rev = b.run(adjs[::-1])
+    assert [same(x, y) for x, y in zip(first[::-1], rev)] == [True] * 8
+    for a, r in zip(adjs, first):
+        assert same(r, oracle.aspl(a, nodes=n))
+    b.close()
+
+
+@pytest.mark.parametrize("wc_log2,slots,tile_rows", [(1, 1, 0), (2, 3, 16), (4, 2, 64), (6, 0, 0), (3, 5, 8)])
+def test_chunking_and_tiling_do_not_change_results(wc_log2, slots, tile_rows):
+    """Column chunk width, concurrent slots and row tiles are free choices."""
+    n, d = 3000, 7
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=77), d)
+    ref = oracle.aspl(adj, nodes=n)
+    og.set_tuning(wc_log2=wc_log2, slots=slots, tile_rows=tile_rows, local_kb=1)
+    try:
+        b = og.Batch([og.GraphSpec(adj, nodes=n)])
+        assert same(b.run()[0], ref)
+        b.close()
+    finally:
+        og.set_tuning()
+
+
+def test_config1_default_kind_and_saving():
+    n, d = 1024, 8
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=1), d)
+    assert gpu_aspl(adj, nodes=n) == (5, 1892906, pytest.approx(3.6139609299, abs=5e-11))
+    assert same(gpu_aspl(adj, nodes=n), oracle.aspl(adj, nodes=n))
+
+
+def _big(golden, name):
+    for g in golden["generators"]:
+        if g.get("name") == name:
+            return g
+    pytest.skip("fixture %s not recorded" % name)
+
+
+def test_config2_single_large_graph(golden):
+    g = _big(golden, "single_large_65536")
+    e = gen_record_edges(og, g)
+    assert sha256(e) == g["sha256"]
+    adj = gen_record_adjacency(og, g, e)
+    got = gpu_aspl(adj, nodes=g["nodes"])
+    assert same(got, result_tuple(g["reference"]))
+
+
+def test_config3_symmetric_graph(golden):
+    g = _big(golden, "symmetric_262144")
+    e = gen_record_edges(og, g)
+    assert sha256(e) == g["sha256"]
+    adj = gen_record_adjacency(og, g, e)
+    assert same(gpu_aspl(adj, nodes=g["nodes"], symmetries=g["symmetries"]), result_tuple(g["reference"]))
+
+
+def test_relabelling_invariance_full_size():
+    """Size-independent property at the single-graph benchmark size: renaming
+    vertices changes no result (checks every row/chunk of the big path)."""
+    n, d = 65536, 16
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=9), d)
+    base = gpu_aspl(adj, nodes=n)
+    perm = np.random.default_rng(1).permutation(n).astype(np.int32)
+    inv = np.empty_like(perm)
+    inv[perm] = np.arange(n, dtype=np.int32)
+    adj2 = perm[adj[inv]]
+    assert same(gpu_aspl(adj2, nodes=n), base)
+    assert base[0] < 10 and base[1] > 0
+
+
+def test_out_of_range_adjacency_is_reported():
+    n, d = 64, 3
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=3), d)
+    bad = adj.copy()
+    bad[5, 1] = n + 7
+    with pytest.raises(og.ODPError) as ei:
+        og.set_aspl_batch([og.GraphSpec(bad, nodes=n)])
+    assert ei.value.code == og.ERR_ADJACENCY
+    # the context stays usable
+    assert same(og.set_aspl_batch([og.GraphSpec(adj, nodes=n)])[0], oracle.aspl(adj, nodes=n))
+
+
+def test_drop_in_errors_exit_like_the_reference(tmp_path):
+    code = textwrap.dedent("""
+        import sys; sys.path.insert(0, %r)
+        import odp_gb300 as og
+        og.init_aspl_general_s(10, 3, None, 3)
+    """ % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True)
+    assert r.returncode == 1 and "must be divisible by symmetries" in r.stderr
+    env = dict(os.environ, ODP_ASPL="BFS")
+    code2 = code.replace("init_aspl_general_s(10, 3, None, 3)", "init_aspl_general(10, 3)")
+    r = subprocess.run([sys.executable, "-c", code2], capture_output=True, text=True, env=env)
+    assert r.returncode == 1 and "BFS for CUDA is not implemented" in r.stderr
+
+
+def test_profile_report(tmp_path):
+    code = textwrap.dedent("""
+        import sys; sys.path.insert(0, %r)
+        import odp_gb300 as og
+        e = og.generate_random_general(256, 4, seed=1)
+        adj = og.conv_edge2adjacency_general(256, e, 4)
+        og.init_aspl_general(256, 4)
+        og.set_aspl(adj); og.set_aspl(adj)
+        og.finalize_aspl()
+    """ % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                       env=dict(os.environ, ODP_PROFILE="1"))
+    assert r.returncode == 0
+    assert "Number of Times = 2" in r.stdout and "Algorithm       = MATRIX (CUDA)" in r.stdout
+
+
+def test_reinit_cycles_of_every_variant():
+    """Init/Finalize of different variants back to back (the reference
+    double-frees after a grid_s session)."""
+    w = h = 8
+    e = og.generate_random_grid(w, h, 4, 3, 4, seed=2)
+    adj4 = og.conv_edge2adjacency_grid(w, h, e, 4, 4)
+    r1 = gpu_aspl(adj4, grid=True, width=w, height=h, symmetries=4)
+    adj1 = og.conv_edge2adjacency_grid(w, h, e, 4, 1)
+    r2 = gpu_aspl(adj1, grid=True, width=w, height=h)
+    assert same(r1, r2)
+    assert same(r1, oracle.aspl(adj1, grid=True, width=w, height=h))
+
+
+def test_grid_256x256_fixture(golden):
+    """The 256x256 grid (diameter 140): the reference's own graph, stored
+    compactly because regenerating it takes minutes on a CPU."""
+    import hashlib
+    g = _big(golden, "grid_256x256")
+    z = np.load(os.path.join(ROOT, "tests", "golden", "grid_256x256_d6_l4_seed4.npz"))
+    codes = z["codes"].astype(np.int32)
+    w = h = 256
+    v = np.arange(w * h)[:, None]
+    adj = ((v // h + codes // 9 - 4) * h + (v % h + codes % 9 - 4)).astype(np.int32)
+    assert hashlib.sha256(adj.tobytes()).hexdigest() == bytes(z["adjacency_sha256"]).decode()
+    edges = og.conv_adjacency2edge_grid(w, h, 6, adj)
+    assert sha256(edges) == g["sha256"] == bytes(z["edges_sha256"]).decode()
+    assert same(gpu_aspl(adj, grid=True, width=w, height=h), result_tuple(g["reference"]))

@@ -1,0 +1,98 @@
+"""The library's host utilities (odp.h generators, conversions, 2-opt
+mutate/restore) against the reference's outputs.  CPU only."""
+import ctypes
+import ctypes.util
+
+import numpy as np
+import pytest
+
+import odp_gb300 as og
+from conftest import gen_record_adjacency, gen_record_edges, sha256
+
+
+def test_private_stream_matches_libc_rand():
+    libc = ctypes.CDLL(ctypes.util.find_library("c"))
+    for seed in [0, 1, 2, 4, 12345, 2**31 - 1, 2**31 + 5, 2**32 - 1]:
+        libc.srand(ctypes.c_uint(seed))
+        expect = [libc.rand() for _ in range(5000)]
+        r = og.Rng(seed)
+        assert [r.next() for _ in range(5000)] == expect, seed
+
+
+def test_generators_match_reference_hashes(golden):
+    for g in golden["generators"]:
+        if g.get("big"):
+            continue
+        assert sha256(gen_record_edges(og, g)) == g["sha256"], g
+
+
+def test_libc_stream_generators_match_seeded():
+    og.srand(5)
+    a = og.generate_random_general(96, 6, 4)
+    b = og.generate_random_general(96, 6, 4, seed=5)
+    assert np.array_equal(a, b)
+    og.srand(6)
+    a = og.generate_random_grid(10, 10, 4, 4, 4)
+    b = og.generate_random_grid(10, 10, 4, 4, 4, seed=6)
+    assert np.array_equal(a, b)
+
+
+def test_mutation_traces_match_reference(golden):
+    for m in golden["mutations"]:
+        if m["kind"] == "general":
+            e = og.generate_random_general(m["nodes"], m["degree"], m["symmetries"], seed=m["graph_seed"])
+            adj = og.conv_edge2adjacency_general(m["nodes"], e, m["degree"], m["symmetries"])
+            og.srand(m["seed"])
+            trace = []
+            for _ in range(m["iters"]):
+                r = og.mutate_adjacency_general(m["nodes"], m["degree"], adj, m["symmetries"])
+                trace += list(r.u) + list(r.v) + list(r.u_d) + list(r.v_d)
+        else:
+            e = og.generate_random_grid(m["width"], m["height"], m["degree"], m["length"], m["symmetries"],
+                                        seed=m["graph_seed"])
+            adj = og.conv_edge2adjacency_grid(m["width"], m["height"], e, m["degree"], m["symmetries"])
+            og.srand(m["seed"])
+            trace = []
+            for _ in range(m["iters"]):
+                r = og.mutate_adjacency_grid(m["width"], m["height"], m["degree"], m["length"], adj, m["symmetries"])
+                trace += list(r.u) + list(r.v) + list(r.u_d) + list(r.v_d)
+        assert trace[:8] == m["first_restore"], m
+        assert sha256(np.array(trace)) == m["trace_sha256"], m
+        assert sha256(adj) == m["final_sha256"], m
+
+
+@pytest.mark.parametrize("s", [1, 2, 4])
+def test_restore_undoes_mutate_general(s):
+    n, d = 240, 6
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, s, seed=3), d, s)
+    og.srand(9)
+    for _ in range(200):
+        before = adj.copy()
+        r = og.mutate_adjacency_general(n, d, adj, s)
+        assert not np.array_equal(before, adj) or True
+        og.restore_adjacency_general(r, adj)
+        assert np.array_equal(before, adj)
+        og.mutate_adjacency_general(n, d, adj, s)
+
+
+@pytest.mark.parametrize("s", [1, 2, 4])
+def test_restore_undoes_mutate_grid(s):
+    w = h = 12
+    d, length = 4, 3
+    adj = og.conv_edge2adjacency_grid(w, h, og.generate_random_grid(w, h, d, length, s, seed=4), d, s)
+    og.srand(11)
+    for _ in range(200):
+        before = adj.copy()
+        r = og.mutate_adjacency_grid(w, h, d, length, adj, s)
+        og.restore_adjacency_grid(r, adj)
+        assert np.array_equal(before, adj)
+        og.mutate_adjacency_grid(w, h, d, length, adj, s)
+
+
+@pytest.mark.parametrize("s", [1, 4, 8])
+def test_edge_adjacency_round_trip(s):
+    n, d = 128, 5
+    e = og.generate_random_general(n, d, s, seed=21)
+    adj = og.conv_edge2adjacency_general(n, e, d, s)
+    e2 = og.conv_adjacency2edge_general(n, d, adj, s)
+    assert np.array_equal(og.conv_edge2adjacency_general(n, e2, d, s), adj)
