@@ -544,3 +544,4 @@ int gbx_event_elapsed_ms(void *start, void *stop, float *ms)
 }
 
 }  /* extern "C" */
+
