@@ -87,6 +87,27 @@ int    ODPX_Rng_next(void *rng_state);
 void   ODPX_Mutate_adjacency_general_s_rng(void *rng_state, int nodes, int degree, const int *num_degrees,
                                            int symmetries, ODP_Restore *r, int *adjacency);
 
+/* ODPX_Set_aspl_noalloc: no counterpart in the reference.  Evaluates one
+ * regular general graph (the arguments of ODP_Init_aspl_general[_s] with
+ * num_degrees == NULL, plus ODP_Set_aspl's host adjacency and outputs)
+ * without allocating any memory, host or device: for callers that must not
+ * allocate while they run, such as an annealing loop on a latency budget
+ * (cudaMalloc and cudaFree synchronise the device and stall its other
+ * streams) or a process whose device memory is already reserved by another
+ * framework's pool allocator.  All working memory comes from one fixed
+ * array of ODPX_NOALLOC_SCRATCH_BYTES in the library's device image, which
+ * every GPU context that loads the library holds until the process exits.
+ * Graphs whose working set does not fit are refused with ODPX_ERR_MEMORY
+ * (a line on stderr says so); as a guide, n = 8192 with degree 32 fits, and
+ * n = 262144 with degree 16 does not.  The first call on each device looks
+ * up the array's device address, so make that first call before any stream
+ * capture.  Every call uses the same array (each call rewrites the state it
+ * needs): calls that overlap on the GPU, from several host threads, race.
+ * Results equal ODP_Set_aspl's bit for bit.  Returns ODPX_*. */
+#define ODPX_NOALLOC_SCRATCH_BYTES (16u << 20)
+int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, const int *adjacency,
+                          int *diameter, long *sum, double *ASPL);
+
 /* Library version string. */
 const char *ODPX_Version(void);
 

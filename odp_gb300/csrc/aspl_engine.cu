@@ -545,3 +545,192 @@ int gbx_event_elapsed_ms(void *start, void *stop, float *ms)
 
 }  /* extern "C" */
 
+/* ---------------------------------------------------------------------- */
+/* Evaluation without any memory allocation: ODPX_Set_aspl_noalloc.        */
+/*                                                                         */
+/* Some callers cannot allocate device memory while they run: an annealing  */
+/* loop on a latency budget, where cudaMalloc/cudaFree synchronise the      */
+/* device and stall its other streams, or a process whose device memory is  */
+/* already reserved by another framework's pool allocator, so an allocation */
+/* could fail in the middle of a run.  This entry point runs the same two   */
+/* kernels as ODP_Set_aspl (expand_kernel, engine_kernel) with all of their */
+/* working memory -- the adjacency copy, the neighbour table, the engine    */
+/* state and the bitset buffers -- carved out of one fixed array that is    */
+/* part of the library's device image.  Every GPU context that loads the    */
+/* library holds that array (ODPX_NOALLOC_SCRATCH_BYTES) until the process  */
+/* exits.                                                                   */
+/* ---------------------------------------------------------------------- */
+
+#include <stdio.h>
+#include <string.h>
+#include <float.h>
+#include <limits.h>
+#include "odp_gb300.h"
+
+#define NOALLOC_MAX_JOBS 256
+#define NOALLOC_MAX_DEVICES 64
+
+namespace {
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[ODPX_NOALLOC_SCRATCH_BYTES];
+
+struct NoallocDevice {
+  int ready;
+  int blocks;
+  unsigned char *scratch;    /* device address of g_noalloc_scratch on this device */
+};
+NoallocDevice g_noalloc_dev[NOALLOC_MAX_DEVICES];
+
+/* Once per device, with that device current: look up the array's device
+ * address (the name is only a host-side stand-in) and the persistent grid
+ * size.  No allocation is involved. */
+int noalloc_device(NoallocDevice **out)
+{
+  int dev = 0;
+  if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= NOALLOC_MAX_DEVICES) return ODPX_ERR_CUDA;
+  NoallocDevice *nd = &g_noalloc_dev[dev];
+  if(!nd->ready){
+    void *p = nullptr;
+    if(cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return ODPX_ERR_CUDA;
+    int sms = 0, per_sm = 0;
+    if(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ODPX_ERR_CUDA;
+    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, 0) != cudaSuccess)
+      return ODPX_ERR_CUDA;
+    nd->scratch = (unsigned char *)p;
+    nd->blocks = (per_sm < 1 ? 1 : per_sm) * sms;
+    nd->ready = 1;
+  }
+  *out = nd;
+  return 0;
+}
+
+inline size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+}  // namespace
+
+extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, const int *adjacency,
+                                     int *diameter, long *sum, double *ASPL)
+{
+  if(nodes <= 0 || degree < 0 || symmetries <= 0 || nodes % symmetries != 0 || !adjacency || !diameter ||
+     !sum || !ASPL)
+    return ODPX_ERR_INVALID;
+  const int n = nodes, d = degree, s = symmetries, B = n / s, W = (B + 63) / 64;
+  const int dp = ((d > 0 ? d : 1) + 3) & ~3;
+  int full_l2 = 1;
+  while((1 << full_l2) < W) full_l2++;
+
+  /* Layout of the scratch array for the widest chunk (<= 64 words) that fits. */
+  size_t off_adj = 0, off_nbr = 0, off_desc = 0, off_jobs = 0, off_state = 0, off_buf = 0, total = 0;
+  size_t out_off = 0, acc_off = 0, levels_off = 0, state_bytes = 0;
+  int wl = full_l2 < 6 ? full_l2 : 6, njobs = 0, nslots = 0, fits = 0;
+  for(; wl >= 1; wl--){
+    njobs = (W + (1 << wl) - 1) >> wl;
+    if(njobs > NOALLOC_MAX_JOBS) break;
+    nslots = njobs < 2 ? njobs : 2;
+    off_adj = 0;
+    off_nbr = up256(off_adj + sizeof(int) * (size_t)B * d);
+    off_desc = up256(off_nbr + sizeof(int) * (size_t)n * dp);
+    off_jobs = up256(off_desc + sizeof(gbx_expand_desc));
+    off_state = up256(off_jobs + sizeof(gbx_job) * (size_t)njobs);
+    out_off = sizeof(gbx_slot) * (size_t)nslots;
+    acc_off = out_off + sizeof(gbx_ctrl) + 64;
+    levels_off = acc_off + 64;
+    state_bytes = levels_off + sizeof(int) * (size_t)njobs;
+    off_buf = up256(off_state + state_bytes);
+    total = off_buf + sizeof(unsigned long long) * 2 * (size_t)nslots * ((size_t)n << wl);
+    if(total <= ODPX_NOALLOC_SCRATCH_BYTES){ fits = 1; break; }
+  }
+  if(!fits){
+    fprintf(stderr, "ODPX_Set_aspl_noalloc: a graph with %d nodes, degree %d and %d symmetries needs more than "
+            "the %u bytes of fixed scratch memory\n", n, d, s, (unsigned)ODPX_NOALLOC_SCRATCH_BYTES);
+    return ODPX_ERR_MEMORY;
+  }
+
+  NoallocDevice *nd = nullptr;
+  int rc = noalloc_device(&nd);
+  if(rc) return rc;
+  unsigned char *base = nd->scratch;
+  cudaStream_t st = cudaStreamPerThread;
+  const int wc = 1 << wl;
+
+  /* Host-side descriptors live on the stack. */
+  gbx_expand_desc desc = {};
+  desc.adj = (const int *)(base + off_adj);
+  desc.ndeg = nullptr;
+  desc.itable = nullptr;
+  desc.nbr = (int *)(base + off_nbr);
+  desc.n = n; desc.d = d; desc.dp = dp; desc.s = s;
+  desc.first_vertex = 0;
+  gbx_job jobs[NOALLOC_MAX_JOBS];
+  const double level_bytes = (double)n * wc * 8.0 * (d + 2);
+  const int vpr = wc / 2, g = vpr < 32 ? vpr : 32, rpp = 8 * (32 / g);
+  int tile_rows = n;
+  if(level_bytes > 96.0 * 1024.0){
+    int tr = (int)(256.0 * 1024.0 / ((double)wc * 8.0 * (d + 2)));
+    if(tr < rpp) tr = rpp;
+    tile_rows = ((tr + rpp - 1) / rpp) * rpp;
+    if(tile_rows > n) tile_rows = n;
+  }
+  for(int k = 0; k < njobs; k++){
+    gbx_job &j = jobs[k];
+    j = gbx_job();
+    j.nbr = desc.nbr;
+    j.n = n; j.dp = dp; j.wc_log2 = wl;
+    j.src0 = k * wc * 64;
+    j.nsrc = B - j.src0 < wc * 64 ? B - j.src0 : wc * 64;
+    j.sym = s; j.graph = 0;
+    j.tile_rows = tile_rows;
+    j.ntiles = (n + tile_rows - 1) / tile_rows;
+  }
+  /* The array keeps whatever the previous call left in it: the engine state
+   * is rewritten here in full; the neighbour table and the bitset buffers
+   * are overwritten by the kernels before they are read. */
+  unsigned char state[sizeof(gbx_slot) * 2 + sizeof(gbx_ctrl) + 64 + 64 + sizeof(int) * NOALLOC_MAX_JOBS];
+  memset(state, 0, sizeof(state));
+  gbx_slot *sl = (gbx_slot *)state;
+  unsigned long long *bufs = (unsigned long long *)(base + off_buf);
+  for(int k = 0; k < nslots; k++){
+    sl[k].ticket = (unsigned long long)jobs[k].ntiles << 32;
+    sl[k].job = k;
+    sl[k].level = 1;
+    sl[k].prev = (unsigned long long)jobs[k].nsrc;
+    sl[k].sum = ((long long)n * jobs[k].nsrc - jobs[k].nsrc) * s;
+    sl[k].buf0 = bufs + (size_t)k * 2 * ((size_t)n << wl);
+    sl[k].buf1 = sl[k].buf0 + ((size_t)n << wl);
+  }
+  ((gbx_ctrl *)(state + out_off))->next_job = (unsigned)nslots;
+
+  if(cudaMemcpyAsync(base + off_adj, adjacency, sizeof(int) * (size_t)B * d, cudaMemcpyHostToDevice, st) ||
+     cudaMemcpyAsync(base + off_desc, &desc, sizeof(desc), cudaMemcpyHostToDevice, st) ||
+     cudaMemcpyAsync(base + off_jobs, jobs, sizeof(gbx_job) * (size_t)njobs, cudaMemcpyHostToDevice, st) ||
+     cudaMemcpyAsync(base + off_state, state, state_bytes, cudaMemcpyHostToDevice, st))
+    return ODPX_ERR_CUDA;
+  unsigned int *d_err = (unsigned int *)(base + off_state + out_off + sizeof(gbx_ctrl));
+  long long eblocks = ((long long)n + 255) / 256;
+  if(eblocks > 65535LL * 8) eblocks = 65535LL * 8;
+  expand_kernel<<<(unsigned)eblocks, 256, 0, st>>>((const gbx_expand_desc *)(base + off_desc), 1, n, d_err);
+  engine_kernel<<<nd->blocks, ENGINE_THREADS, 0, st>>>(
+      (const gbx_job *)(base + off_jobs), njobs, (gbx_slot *)(base + off_state), nslots,
+      (gbx_ctrl *)(base + off_state + out_off), (gbx_graph_acc *)(base + off_state + acc_off),
+      (int *)(base + off_state + levels_off), 60ull * 1000000000ull);
+  if(cudaGetLastError() != cudaSuccess) return ODPX_ERR_CUDA;
+  unsigned char out[sizeof(gbx_ctrl) + 64 + 64];
+  if(cudaMemcpyAsync(out, base + off_state + out_off, sizeof(out), cudaMemcpyDeviceToHost, st) ||
+     cudaStreamSynchronize(st))
+    return ODPX_ERR_CUDA;
+  const unsigned int err = ((const gbx_ctrl *)out)->error | *(const unsigned int *)(out + sizeof(gbx_ctrl));
+  if(err & GBX_ERR_TIMEOUT) return ODPX_ERR_TIMEOUT;
+  if(err & GBX_ERR_BAD_ADJ) return ODPX_ERR_ADJACENCY;
+  const gbx_graph_acc *acc = (const gbx_graph_acc *)(out + sizeof(gbx_ctrl) + 64);
+  if(acc->flags & 1){
+    *diameter = INT_MAX;
+    *sum = LONG_MAX;
+    *ASPL = DBL_MAX;
+    return 0;
+  }
+  long total_sum = (long)acc->sum;
+  *diameter = acc->levels;
+  *ASPL = total_sum / (((double)n - 1) * n);
+  *sum = (long)(total_sum / 2.0);
+  return 0;
+}
