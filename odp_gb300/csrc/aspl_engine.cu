@@ -43,6 +43,9 @@
 
 #define ENGINE_THREADS 256
 #define ENGINE_WARPS (ENGINE_THREADS / 32)
+#ifndef ENGINE_MIN_BLOCKS
+#define ENGINE_MIN_BLOCKS 4         /* resident CTAs per SM the register budget is sized for */
+#endif
 
 namespace {
 
@@ -180,69 +183,75 @@ __device__ __forceinline__ void mark_source(uint4 (&acc)[RowShape<WC>::V], int b
   }
 }
 
-/* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources. */
+/* Shared-memory budget for one block of neighbour lists (ints). */
+#define IDX_SMEM_INTS 4096
+
+/* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources.
+ * sidx holds the neighbour lists of rows [row0, row0 + nrows). */
 template <int WC>
-__device__ unsigned rows_level1(const gbx_job &jb, unsigned long long *Y, int r0, int r1)
+__device__ unsigned rows_level1(const int *sidx, int dp, int src0, int nsrc, unsigned long long *Y, int row0,
+                                int nrows)
 {
   typedef RowShape<WC> S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
-  const int dp = jb.dp, src0 = jb.src0, nsrc = jb.nsrc;
   unsigned cnt = 0;
-  for(int row = r0 + warp * S::RPW + sub; row < r1; row += ENGINE_WARPS * S::RPW){
+  for(int r = warp * S::RPW + sub; r < nrows; r += ENGINE_WARPS * S::RPW){
+    const int row = row0 + r;
     uint4 acc[S::V];
 #pragma unroll
     for(int k = 0; k < S::V; k++) acc[k] = make_uint4(0u, 0u, 0u, 0u);
     mark_source<WC>(acc, row - src0, nsrc, gl);
-    const int4 *ip = reinterpret_cast<const int4 *>(jb.nbr + (size_t)row * dp);
+    const int4 *ip = reinterpret_cast<const int4 *>(sidx + r * dp);
     for(int j = 0; j < (dp >> 2); j++){
-      int4 q = __ldg(ip + j);
+      int4 q = ip[j];
       mark_source<WC>(acc, q.x - src0, nsrc, gl);
       mark_source<WC>(acc, q.y - src0, nsrc, gl);
       mark_source<WC>(acc, q.z - src0, nsrc, gl);
       mark_source<WC>(acc, q.w - src0, nsrc, gl);
     }
-    uint4 *yr = reinterpret_cast<uint4 *>(Y + (size_t)row * WC);
+    uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
 #pragma unroll
     for(int k = 0; k < S::V; k++){
-      __stcg(yr + gl + k * S::G, acc[k]);
+      __stcg(yr + k * S::G, acc[k]);
       cnt += popc4(acc[k]);
     }
   }
   return cnt;
 }
 
-/* Level k >= 2: P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]]. */
+/* Level k >= 2: P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]].  Indices come
+ * from shared memory, so a row's gathers issue back to back: every step
+ * keeps eight 16-byte loads per lane in flight (NB neighbours x V vectors). */
 template <int WC>
-__device__ unsigned rows_levelk(const gbx_job &jb, const unsigned long long *X, unsigned long long *Y,
-                                int r0, int r1)
+__device__ unsigned rows_levelk(const int *sidx, int dp, const unsigned long long *X, unsigned long long *Y,
+                                int row0, int nrows)
 {
   typedef RowShape<WC> S;
+  constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;       /* neighbours gathered per step */
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
-  const int dp = jb.dp;
   const uint4 *Xv = reinterpret_cast<const uint4 *>(X);
   unsigned cnt = 0;
-  for(int row = r0 + warp * S::RPW + sub; row < r1; row += ENGINE_WARPS * S::RPW){
+  for(int r = warp * S::RPW + sub; r < nrows; r += ENGINE_WARPS * S::RPW){
+    const int row = row0 + r;
     uint4 acc[S::V];
     const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
 #pragma unroll
     for(int k = 0; k < S::V; k++) acc[k] = __ldcg(xr + k * S::G);
-    const int4 *ip = reinterpret_cast<const int4 *>(jb.nbr + (size_t)row * dp);
-#pragma unroll 2
-    for(int j = 0; j < (dp >> 2); j++){
-      const int4 q = __ldg(ip + j);
-      uint4 t[4][S::V];
-      const int idx[4] = {q.x, q.y, q.z, q.w};
+    const int *ip = sidx + r * dp;
+    for(int j = 0; j < dp; j += NB){
+      uint4 t[NB][S::V];
 #pragma unroll
-      for(int i = 0; i < 4; i++){
-        const uint4 *nr = Xv + (size_t)(idx[i] < 0 ? 0 : idx[i]) * S::VPR + gl;
+      for(int i = 0; i < NB; i++){
+        const int idx = (j + i < dp) ? ip[j + i] : -1;
+        const uint4 *nr = Xv + (size_t)(idx < 0 ? 0 : idx) * S::VPR + gl;
 #pragma unroll
         for(int k = 0; k < S::V; k++)
-          t[i][k] = (idx[i] >= 0) ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+          t[i][k] = (idx >= 0) ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
       }
 #pragma unroll
-      for(int i = 0; i < 4; i++)
+      for(int i = 0; i < NB; i++)
 #pragma unroll
         for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
     }
@@ -256,24 +265,67 @@ __device__ unsigned rows_levelk(const gbx_job &jb, const unsigned long long *X, 
   return cnt;
 }
 
-__device__ unsigned run_rows(const gbx_job &jb, int level, const unsigned long long *X, unsigned long long *Y,
-                             int r0, int r1)
+template <int WC>
+__device__ unsigned run_block(const int *sidx, int dp, const gbx_job &jb, int level, const unsigned long long *X,
+                              unsigned long long *Y, int row0, int nrows)
 {
-#define ODP_WC_CASE(L) case L: return level == 1 ? rows_level1<(1 << L)>(jb, Y, r0, r1) \
-                                                 : rows_levelk<(1 << L)>(jb, X, Y, r0, r1);
-  switch(jb.wc_log2){
-    ODP_WC_CASE(1) ODP_WC_CASE(2) ODP_WC_CASE(3) ODP_WC_CASE(4)
-    ODP_WC_CASE(5) ODP_WC_CASE(6) ODP_WC_CASE(7) ODP_WC_CASE(8)
-    default: return 0;
-  }
+  return level == 1 ? rows_level1<WC>(sidx, dp, jb.src0, jb.nsrc, Y, row0, nrows)
+                    : rows_levelk<WC>(sidx, dp, X, Y, row0, nrows);
+}
+
+/* Rows [r0, r1) of one level: neighbour lists are staged block by block in
+ * shared memory (one coalesced pass per block), then the block's rows are
+ * processed.  Returns this thread's popcount. */
+__device__ unsigned run_rows(int *sidx, const gbx_job &jb, int level, const unsigned long long *X,
+                             unsigned long long *Y, int r0, int r1)
+{
+  const int dp = jb.dp;
+  const int block_rows = IDX_SMEM_INTS / dp;
+  unsigned cnt = 0;
+  for(int b0 = r0; b0 < r1; b0 += block_rows){
+    const int nr = min(block_rows, r1 - b0);
+    const int4 *src = reinterpret_cast<const int4 *>(jb.nbr + (size_t)b0 * dp);
+    int4 *dst = reinterpret_cast<int4 *>(sidx);
+    for(int i = threadIdx.x; i < (nr * dp) >> 2; i += ENGINE_THREADS) dst[i] = __ldg(src + i);
+    __syncthreads();
+#define ODP_WC_CASE(L) case L: cnt += run_block<(1 << L)>(sidx, dp, jb, level, X, Y, b0, nr); break;
+    switch(jb.wc_log2){
+      ODP_WC_CASE(1) ODP_WC_CASE(2) ODP_WC_CASE(3) ODP_WC_CASE(4)
+      ODP_WC_CASE(5) ODP_WC_CASE(6) ODP_WC_CASE(7) ODP_WC_CASE(8)
+      default: break;
+    }
 #undef ODP_WC_CASE
+    __syncthreads();
+  }
+  return cnt;
 }
 
 /* ---------------------------------------------------------------------- */
 /* Persistent engine.                                                      */
 /* ---------------------------------------------------------------------- */
 
-__global__ void __launch_bounds__(ENGINE_THREADS)
+/* Takes one tile from the first slot (from `cursor` on) that has one left.
+ * The ticket is read before it is incremented, so slots without tiles are
+ * never pushed past their tile count by idle CTAs.  Thread 0 only. */
+__device__ __forceinline__ bool take_tile(gbx_slot *slots, int nslots, int &cursor, int &slot, int &tile)
+{
+  for(int i = 0; i < nslots; i++){
+    int si = cursor + i;
+    if(si >= nslots) si -= nslots;
+    gbx_slot *sl = &slots[si];
+    unsigned long long t = vload(&sl->ticket);
+    if((unsigned)t >= (unsigned)(t >> 32)) continue;
+    t = atomicAdd(&sl->ticket, 1ull);
+    if((unsigned)t >= (unsigned)(t >> 32)) continue;
+    slot = si;
+    tile = (int)(unsigned)t;
+    cursor = si;
+    return true;
+  }
+  return false;
+}
+
+__global__ void __launch_bounds__(ENGINE_THREADS, ENGINE_MIN_BLOCKS)
 engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int nslots, gbx_ctrl *ctrl,
               gbx_graph_acc *acc, int *job_levels, unsigned long long spin_limit_ns)
 {
@@ -281,32 +333,35 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   __shared__ int sh_state, sh_slot, sh_tile, sh_level;
   __shared__ unsigned long long *sh_buf0, *sh_buf1;
   __shared__ unsigned sh_warp[ENGINE_WARPS];
+  __shared__ __align__(16) int sh_idx[IDX_SMEM_INTS];
 
   int cursor = blockIdx.x % nslots;
   unsigned long long idle_since = 0;
+  int pre_slot = -1, pre_tile = 0;      /* thread 0: a ticket taken ahead of time */
 
   for(;;){
     if(threadIdx.x == 0){
-      int state = 0;
-      for(int i = 0; i < nslots && state == 0; i++){
-        int si = cursor + i;
-        if(si >= nslots) si -= nslots;
-        gbx_slot *sl = &slots[si];
-        unsigned long long t = vload(&sl->ticket);
-        if((unsigned)t >= (unsigned)(t >> 32)) continue;
-        t = atomicAdd(&sl->ticket, 1ull);
-        if((unsigned)t >= (unsigned)(t >> 32)) continue;
+      int state = 0, slot = -1, tile = 0;
+      if(pre_slot >= 0){ slot = pre_slot; tile = pre_tile; pre_slot = -1; state = 1; }
+      else if(take_tile(slots, nslots, cursor, slot, tile)) state = 1;
+      if(state == 1){
         __threadfence();                               /* acquire the level's inputs */
-        sh_slot = si;
-        sh_tile = (int)(unsigned)t;
+        gbx_slot *sl = &slots[slot];
+        sh_slot = slot;
+        sh_tile = tile;
         sh_level = vload(&sl->level);
         sh_job = jobs[vload(&sl->job)];
         sh_buf0 = vload(&sl->buf0);
         sh_buf1 = vload(&sl->buf1);
-        cursor = si;
-        state = 1;
+        idle_since = 0;
+        /* Take the next ticket now so its round trip overlaps this tile.  Not
+         * for one-tile jobs: their CTA keeps going level after level. */
+        if(sh_job.ntiles > 1){
+          int s2, t2;
+          if(take_tile(slots, nslots, cursor, s2, t2)){ pre_slot = s2; pre_tile = t2; }
+        }
       }
-      if(state == 0){
+      else{
         if(vload(&ctrl->retired) >= (unsigned)nslots || (vload(&ctrl->error) & GBX_ERR_TIMEOUT)){
           state = 2;
         }
@@ -320,7 +375,6 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
           else __nanosleep(256);
         }
       }
-      else idle_since = 0;
       sh_state = state;
     }
     __syncthreads();
@@ -329,8 +383,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
     if(state == 0){ __syncthreads(); continue; }
 
     const gbx_job jb = sh_job;
-    const int si = sh_slot;
-    gbx_slot *sl = &slots[si];
+    gbx_slot *sl = &slots[sh_slot];
     unsigned long long *buf0 = sh_buf0, *buf1 = sh_buf1;
     int level = sh_level, tile = sh_tile;
     __syncthreads();
@@ -341,7 +394,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
       unsigned long long *Y = (level & 1) ? buf1 : buf0;
       const int r0 = tile * jb.tile_rows;
       const int r1 = min(r0 + jb.tile_rows, jb.n);
-      unsigned cnt = run_rows(jb, level, X, Y, r0, r1);
+      unsigned cnt = run_rows(sh_idx, jb, level, X, Y, r0, r1);
       cnt = __reduce_add_sync(0xffffffffu, cnt);
       if((threadIdx.x & 31) == 0) sh_warp[threadIdx.x >> 5] = cnt;
       __threadfence();                                 /* release this thread's row writes */
