@@ -99,6 +99,8 @@ def load():
         "ODPX_Batch_info": (I, [P, I, IP, IP, IP, IP]),
         "ODPX_Batch_job_levels": (I, [P, IP, I]),
         "ODPX_Batch_set_wait_limit": (None, [P, ctypes.c_ulonglong]),
+        "ODPX_Batch_bytes_alg": (ctypes.c_double, [P]),
+        "ODPX_Measure_l2_read_gbs": (ctypes.c_double, [I, I]),
         "ODPX_Set_tuning": (None, [I, I, I, I, I, I]),
         "ODPX_Current_plan": (P, []),
         "ODPX_Rng_size": (ctypes.c_size_t, []),
@@ -397,6 +399,10 @@ class Batch:
         load().ODPX_Batch_job_levels(self._h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
         return out
 
+    def bytes_alg(self):
+        """Algorithmic bytes of the last run (roofline numerator)."""
+        return float(load().ODPX_Batch_bytes_alg(self._h))
+
     def set_wait_limit(self, ns):
         load().ODPX_Batch_set_wait_limit(self._h, int(ns))
 
@@ -419,3 +425,8 @@ def set_tuning(wc_log2=0, slots=0, tile_rows=0, l2_budget_mb=0, local_kb=0, use_
 
 def version():
     return load().ODPX_Version().decode()
+
+
+def measure_l2_read_gbs(megabytes=48, reps=50):
+    """Read bandwidth (GB/s) of an L2-resident stream: the L2 roofline ceiling."""
+    return float(load().ODPX_Measure_l2_read_gbs(megabytes, reps))

@@ -462,6 +462,21 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   }
 }
 
+/* L2 read ceiling for the roofline: every CTA streams an L2-resident buffer
+ * with the same 16-byte ld.global.cg loads the engine uses, `reps` times. */
+__global__ void __launch_bounds__(256) l2_read_probe_kernel(const uint4 *__restrict__ buf, size_t vecs, int reps,
+                                                             unsigned *sink)
+{
+  uint4 acc = make_uint4(0u, 0u, 0u, 0u);
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for(int r = 0; r < reps; r++)
+    for(size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < vecs; i += stride){
+      uint4 v = __ldcg(buf + i);
+      acc.x ^= v.x; acc.y ^= v.y; acc.z ^= v.z; acc.w ^= v.w;
+    }
+  if((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9e3779b9u) sink[0] = 1;   /* keeps the loads */
+}
+
 int g_engine_blocks = 0;
 
 }  // namespace
@@ -494,6 +509,35 @@ int gbx_device_init(int *sm_count)
 }
 
 int gbx_engine_blocks(void) { return g_engine_blocks; }
+
+int gbx_l2_read_probe(size_t bytes, int reps, double *gbs)
+{
+  void *buf = nullptr, *sink = nullptr;
+  cudaEvent_t a, b;
+  cudaError_t e = cudaMalloc(&buf, bytes);
+  if(e != cudaSuccess) return (int)e;
+  if((e = cudaMalloc(&sink, 64)) != cudaSuccess){ cudaFree(buf); return (int)e; }
+  cudaMemset(buf, 0x5a, bytes);
+  cudaEventCreate(&a);
+  cudaEventCreate(&b);
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const size_t vecs = bytes / 16;
+  l2_read_probe_kernel<<<sms * 8, 256>>>((const uint4 *)buf, vecs, 1, (unsigned *)sink);   /* warm L2 */
+  cudaEventRecord(a);
+  l2_read_probe_kernel<<<sms * 8, 256>>>((const uint4 *)buf, vecs, reps, (unsigned *)sink);
+  cudaEventRecord(b);
+  e = cudaEventSynchronize(b);
+  float ms = 0;
+  if(e == cudaSuccess) e = cudaEventElapsedTime(&ms, a, b);
+  if(e == cudaSuccess) *gbs = (double)bytes * reps / (ms * 1e-3) / 1e9;
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  cudaFree(sink);
+  cudaFree(buf);
+  return (int)e;
+}
 
 int gbx_malloc(void **p, size_t bytes) { return (int)cudaMalloc(p, bytes ? bytes : 256); }
 int gbx_free(void *p) { return p ? (int)cudaFree(p) : 0; }

@@ -233,3 +233,13 @@ void ODPX_Batch_set_wait_limit(ODPX_Batch *batch, unsigned long long ns)
 {
   if(batch) batch->spin_limit_ns = ns;
 }
+
+double ODPX_Batch_bytes_alg(const ODPX_Batch *batch) { return batch ? odp_plan_bytes_alg(batch) : 0.0; }
+
+double ODPX_Measure_l2_read_gbs(int megabytes, int reps)
+{
+  double gbs = 0;
+  if(odp_device_ready()) return -1.0;
+  if(gbx_l2_read_probe((size_t)megabytes << 20, reps, &gbs)) return -1.0;
+  return gbs;
+}

@@ -193,14 +193,12 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     int full_l2 = ilog2_ceil(g->W < 2 ? 2 : g->W);
     int wl;
     if(tuning->wc_log2 > 0) wl = tuning->wc_log2;
-    else if(count > 1) wl = full_l2 < 7 ? full_l2 : 7;          /* batch: whole rows up to 1 KB */
     else{
-      /* single graph: widest chunk (<= 512 B rows) whose two buffers, for
-       * two concurrently active chunks, fit the L2 budget; very large n
-       * streams from HBM with 256 B rows */
-      wl = full_l2 < 6 ? full_l2 : 6;
-      while(wl > 3 && 2.0 * 2.0 * g->n * (double)(1 << wl) * 8.0 > budget) wl--;
-      if(2.0 * 2.0 * g->n * (double)(1 << wl) * 8.0 > budget) wl = full_l2 < 5 ? full_l2 : 5;
+      /* 128-byte rows (16 words): measured on GB300 to beat wider rows at
+       * equal L2 footprint, because more chunks can be in flight (several
+       * slots) and their level boundaries overlap; in a batch it also keeps
+       * every job's working set at or below 2 MB for n <= 8192 */
+      wl = full_l2 < 4 ? full_l2 : 4;
     }
     if(wl < 1) wl = 1;
     if(wl > 8) wl = 8;
@@ -214,7 +212,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     else if(level_bytes <= local_bytes) g->tile_rows = g->n;
     else{
       double per_row = (double)wc * 8.0 * (g->d + 2);
-      int tr = (int)(256.0 * 1024.0 / per_row);
+      int tr = (int)(288.0 * 1024.0 / per_row);
       g->tile_rows = ALIGN_UP(tr < rpp ? rpp : tr, rpp);
     }
     if(g->tile_rows > g->n) g->tile_rows = g->n;
@@ -272,6 +270,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   int nslots = tuning->slots > 0 ? tuning->slots : fit;
   if(tuning->slots <= 0){
     if(nslots < 2) nslots = 2;
+    if(count == 1 && nslots > 4) nslots = 4;
     if(count > 1 && nslots < 32) nslots = 32;
     if(nslots > 512) nslots = 512;
   }
@@ -308,7 +307,12 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     long long first = 0;
     for(int i = 0; i < count; i++){
       odp_plan_graph *g = &p->g[i];
-      if(g->has_ndeg) fill_degrees(&shapes[i], g->n, h_nd + g->ndeg_off);
+      if(g->has_ndeg){
+        fill_degrees(&shapes[i], g->n, h_nd + g->ndeg_off);
+        g->row_reads = 0;
+        for(int v = 0; v < g->n; v++) g->row_reads += (double)h_nd[g->ndeg_off + v] + 2.0;
+      }
+      else g->row_reads = (double)g->n * (g->d + 2);
       if(g->has_itable) fill_itable(g->width, g->height, g->s, h_it + g->itable_off);
       gbx_expand_desc *e = &ed[i];
       e->adj = p->d_adj + g->adj_off;
@@ -458,4 +462,16 @@ unsigned int odp_plan_error(const odp_plan *p)
 {
   const gbx_ctrl *ctrl = (const gbx_ctrl *)p->h_state_out;
   return *(const unsigned int *)(p->h_state_out + sizeof(gbx_ctrl)) | ctrl->error;
+}
+
+double odp_plan_bytes_alg(const odp_plan *p)
+{
+  const int *lv = odp_plan_job_levels(p);
+  double total = 0;
+  for(int k = 0; k < p->njobs; k++){
+    const gbx_job *j = &p->h_jobs[k];
+    int l = lv[k] < 0 ? -lv[k] : lv[k];
+    total += (double)l * 8.0 * (double)(1 << j->wc_log2) * p->g[j->graph].row_reads;
+  }
+  return total;
 }

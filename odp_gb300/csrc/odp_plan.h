@@ -37,6 +37,7 @@ typedef struct {
   size_t adj_off, ndeg_off, itable_off, nbr_off;   /* int offsets into packed arrays */
   size_t adj_ints;
   int has_ndeg, has_itable;
+  double row_reads;            /* sum over vertices of (degree + 2): rows touched per row per level */
 } odp_plan_graph;
 
 typedef struct odp_plan {
@@ -86,6 +87,9 @@ unsigned int odp_plan_error(const odp_plan *p);
 /* Level at which each job (in plan order) finished; negative if it stalled. */
 const int *odp_plan_job_levels(const odp_plan *p);
 int odp_plan_enqueue_engine(odp_plan *p);
+/* Algorithmic bytes of the last run: sum over jobs of
+ * |level| x 8 x words-per-row x row_reads of the job's graph. */
+double odp_plan_bytes_alg(const odp_plan *p);
 
 /* Device bring-up shared by every entry point; exits through ODP_FAIL-like
  * reporting on failure when `fatal`. */
