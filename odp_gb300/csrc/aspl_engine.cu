@@ -185,47 +185,80 @@ __device__ __forceinline__ void mark_source(uint4 (&acc)[RowShape<WC>::V], int b
 
 /* Shared-memory budget for one block of neighbour lists (ints). */
 #define IDX_SMEM_INTS 4096
+#define BLOCK_ROWS_MAX (IDX_SMEM_INTS / 4)
 
-/* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources.
- * sidx holds the neighbour lists of rows [row0, row0 + nrows). */
+/* Per-block staging area: the block's neighbour lists, the previous level's
+ * change masks of those neighbours, and per row its own previous mask and
+ * the union of both (rows whose lanes have nothing to do are skipped). */
+struct Stage {
+  int idx[IDX_SMEM_INTS];
+  unsigned nmask[IDX_SMEM_INTS];
+  unsigned own[BLOCK_ROWS_MAX];
+  unsigned act[BLOCK_ROWS_MAX];
+};
+
+/* Source ordinal of a row (the bit it owns across the chunks). */
+__device__ __forceinline__ int source_of(const int *srcpos, int row)
+{
+  if(row < 0) return -1;
+  return srcpos ? __ldg(srcpos + row) : row;
+}
+
+/* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources, and the
+ * lanes of each row whose words differ from the identity P_0. */
 template <int WC>
-__device__ unsigned rows_level1(const int *sidx, int dp, int src0, int nsrc, unsigned long long *Y, int row0,
-                                int nrows)
+__device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsigned long long *Y,
+                                unsigned *Mcur, int row0, int nrows)
 {
   typedef RowShape<WC> S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
+  const int src0 = jb.src0, nsrc = jb.nsrc;
   unsigned cnt = 0;
-  for(int r = warp * S::RPW + sub; r < nrows; r += ENGINE_WARPS * S::RPW){
-    const int row = row0 + r;
-    uint4 acc[S::V];
+  for(int base = 0; base < nrows; base += ENGINE_WARPS * S::RPW){
+    const int r = base + warp * S::RPW + sub;
+    const bool valid = r < nrows;
+    bool changed = false;
+    if(valid){
+      const int row = row0 + r;
+      uint4 acc[S::V], id[S::V];
 #pragma unroll
-    for(int k = 0; k < S::V; k++) acc[k] = make_uint4(0u, 0u, 0u, 0u);
-    mark_source<WC>(acc, row - src0, nsrc, gl);
-    const int4 *ip = reinterpret_cast<const int4 *>(sidx + r * dp);
-    for(int j = 0; j < (dp >> 2); j++){
-      int4 q = ip[j];
-      mark_source<WC>(acc, q.x - src0, nsrc, gl);
-      mark_source<WC>(acc, q.y - src0, nsrc, gl);
-      mark_source<WC>(acc, q.z - src0, nsrc, gl);
-      mark_source<WC>(acc, q.w - src0, nsrc, gl);
-    }
-    uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
+      for(int k = 0; k < S::V; k++){ acc[k] = make_uint4(0u, 0u, 0u, 0u); id[k] = acc[k]; }
+      const int self = source_of(jb.srcpos, row) - src0;
+      mark_source<WC>(acc, self, nsrc, gl);
+      mark_source<WC>(id, self, nsrc, gl);
+      const int4 *ip = reinterpret_cast<const int4 *>(st.idx + r * dp);
+      for(int j = 0; j < (dp >> 2); j++){
+        int4 q = ip[j];
+        mark_source<WC>(acc, source_of(jb.srcpos, q.x) - src0, nsrc, gl);
+        mark_source<WC>(acc, source_of(jb.srcpos, q.y) - src0, nsrc, gl);
+        mark_source<WC>(acc, source_of(jb.srcpos, q.z) - src0, nsrc, gl);
+        mark_source<WC>(acc, source_of(jb.srcpos, q.w) - src0, nsrc, gl);
+      }
+      uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
 #pragma unroll
-    for(int k = 0; k < S::V; k++){
-      __stcg(yr + k * S::G, acc[k]);
-      cnt += popc4(acc[k]);
+      for(int k = 0; k < S::V; k++){
+        __stcg(yr + k * S::G, acc[k]);
+        cnt += popc4(acc[k]);
+        changed |= (acc[k].x != id[k].x) | (acc[k].y != id[k].y) | (acc[k].z != id[k].z) | (acc[k].w != id[k].w);
+      }
     }
+    const unsigned bal = __ballot_sync(0xffffffffu, changed);
+    if(valid && gl == 0)
+      Mcur[row0 + r] = S::G == 32 ? bal : (bal >> (sub * S::G)) & ((1u << S::G) - 1u);
   }
   return cnt;
 }
 
-/* Level k >= 2: P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]].  Indices come
- * from shared memory, so a row's gathers issue back to back: every step
- * keeps eight 16-byte loads per lane in flight (NB neighbours x V vectors). */
+/* Level k >= 2: P_k[v] = P_{k-1}[v] | OR over neighbours u whose lane words
+ * changed at level k-1 of P_{k-1}[u] (the other neighbours' words are
+ * already in P_{k-1}[v]).  Y still holds P_{k-2}; a lane writes only when
+ * its words differ from that (changed at k-1 or at k), except at level 2,
+ * where Y has never been written and every word is stored.  Returns the bits
+ * added at this level; the row's new change mask goes to Mcur. */
 template <int WC>
-__device__ unsigned rows_levelk(const int *sidx, int dp, const unsigned long long *X, unsigned long long *Y,
-                                int row0, int nrows)
+__device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long long *X, unsigned long long *Y,
+                                unsigned *Mcur, int row0, int nrows, bool write_all)
 {
   typedef RowShape<WC> S;
   constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;       /* neighbours gathered per step */
@@ -233,51 +266,74 @@ __device__ unsigned rows_levelk(const int *sidx, int dp, const unsigned long lon
   const int sub = lane / S::G, gl = lane % S::G;
   const uint4 *Xv = reinterpret_cast<const uint4 *>(X);
   unsigned cnt = 0;
-  for(int r = warp * S::RPW + sub; r < nrows; r += ENGINE_WARPS * S::RPW){
-    const int row = row0 + r;
-    uint4 acc[S::V];
-    const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
+  for(int base = 0; base < nrows; base += ENGINE_WARPS * S::RPW){
+    const int r = base + warp * S::RPW + sub;
+    const bool valid = r < nrows;
+    bool changed = false;
+    if(valid && (write_all || ((st.act[r] >> gl) & 1u))){
+      const int row = row0 + r;
+      const bool own = (st.own[r] >> gl) & 1u;
+      uint4 acc[S::V];
+      const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
+      unsigned before = 0;
 #pragma unroll
-    for(int k = 0; k < S::V; k++) acc[k] = __ldcg(xr + k * S::G);
-    const int *ip = sidx + r * dp;
-    for(int j = 0; j < dp; j += NB){
-      uint4 t[NB][S::V];
+      for(int k = 0; k < S::V; k++){ acc[k] = __ldcg(xr + k * S::G); before += popc4(acc[k]); }
+      unsigned fresh = 0;                              /* any bit new at this level */
+      const int *ip = st.idx + r * dp;
+      const unsigned *mp = st.nmask + r * dp;
+      for(int j = 0; j < dp; j += NB){
+        uint4 t[NB][S::V];
 #pragma unroll
-      for(int i = 0; i < NB; i++){
-        const int idx = (j + i < dp) ? ip[j + i] : -1;
-        const uint4 *nr = Xv + (size_t)(idx < 0 ? 0 : idx) * S::VPR + gl;
+        for(int i = 0; i < NB; i++){
+          const bool take = (j + i < dp) && ((mp[j + i] >> gl) & 1u);
+          const int idx = take ? ip[j + i] : 0;
+          const uint4 *nr = Xv + (size_t)idx * S::VPR + gl;
 #pragma unroll
-        for(int k = 0; k < S::V; k++)
-          t[i][k] = (idx >= 0) ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+          for(int k = 0; k < S::V; k++)
+            t[i][k] = take ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for(int i = 0; i < NB; i++)
+#pragma unroll
+          for(int k = 0; k < S::V; k++){
+            fresh |= (t[i][k].x & ~acc[k].x) | (t[i][k].y & ~acc[k].y) | (t[i][k].z & ~acc[k].z) |
+                     (t[i][k].w & ~acc[k].w);
+            or_into(acc[k], t[i][k]);
+          }
       }
+      unsigned after = 0;
 #pragma unroll
-      for(int i = 0; i < NB; i++)
+      for(int k = 0; k < S::V; k++) after += popc4(acc[k]);
+      const unsigned added = after - before;
+      changed = fresh != 0;
+      if(own || changed || write_all){
+        uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
 #pragma unroll
-        for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
+        for(int k = 0; k < S::V; k++) __stcg(yr + k * S::G, acc[k]);
+      }
+      cnt += added;
     }
-    uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
-#pragma unroll
-    for(int k = 0; k < S::V; k++){
-      __stcg(yr + k * S::G, acc[k]);
-      cnt += popc4(acc[k]);
-    }
+    const unsigned bal = __ballot_sync(0xffffffffu, changed);
+    if(valid && gl == 0)
+      Mcur[row0 + r] = S::G == 32 ? bal : (bal >> (sub * S::G)) & ((1u << S::G) - 1u);
   }
   return cnt;
 }
 
 template <int WC>
-__device__ unsigned run_block(const int *sidx, int dp, const gbx_job &jb, int level, const unsigned long long *X,
-                              unsigned long long *Y, int row0, int nrows)
+__device__ unsigned run_block(const Stage &st, int dp, const gbx_job &jb, int level, const unsigned long long *X,
+                              unsigned long long *Y, unsigned *Mcur, int row0, int nrows)
 {
-  return level == 1 ? rows_level1<WC>(sidx, dp, jb.src0, jb.nsrc, Y, row0, nrows)
-                    : rows_levelk<WC>(sidx, dp, X, Y, row0, nrows);
+  return level == 1 ? rows_level1<WC>(st, dp, jb, Y, Mcur, row0, nrows)
+                    : rows_levelk<WC>(st, dp, X, Y, Mcur, row0, nrows, level == 2);
 }
 
-/* Rows [r0, r1) of one level: neighbour lists are staged block by block in
- * shared memory (one coalesced pass per block), then the block's rows are
- * processed.  Returns this thread's popcount. */
-__device__ unsigned run_rows(int *sidx, const gbx_job &jb, int level, const unsigned long long *X,
-                             unsigned long long *Y, int r0, int r1)
+/* Rows [r0, r1) of one level, block by block: stage the block's neighbour
+ * lists (and, after level 1, the neighbours' and rows' change masks of the
+ * previous level) in shared memory, then process the rows.  Returns this
+ * thread's share of the level's count (level 1: bits set; later: added). */
+__device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsigned long long *X,
+                             unsigned long long *Y, const unsigned *Mprev, unsigned *Mcur, int r0, int r1)
 {
   const int dp = jb.dp;
   const int block_rows = IDX_SMEM_INTS / dp;
@@ -285,13 +341,27 @@ __device__ unsigned run_rows(int *sidx, const gbx_job &jb, int level, const unsi
   for(int b0 = r0; b0 < r1; b0 += block_rows){
     const int nr = min(block_rows, r1 - b0);
     const int4 *src = reinterpret_cast<const int4 *>(jb.nbr + (size_t)b0 * dp);
-    int4 *dst = reinterpret_cast<int4 *>(sidx);
+    int4 *dst = reinterpret_cast<int4 *>(st.idx);
     for(int i = threadIdx.x; i < (nr * dp) >> 2; i += ENGINE_THREADS) dst[i] = __ldg(src + i);
+    if(level > 1){
+      for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS) st.own[r] = __ldcg(Mprev + b0 + r);
+      __syncthreads();
+      for(int i = threadIdx.x; i < nr * dp; i += ENGINE_THREADS){
+        const int q = st.idx[i];
+        st.nmask[i] = q >= 0 ? __ldcg(Mprev + q) : 0u;
+      }
+      __syncthreads();
+      for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS){
+        unsigned a = st.own[r];
+        for(int j = 0; j < dp; j++) a |= st.nmask[r * dp + j];
+        st.act[r] = a;
+      }
+    }
     __syncthreads();
-#define ODP_WC_CASE(L) case L: cnt += run_block<(1 << L)>(sidx, dp, jb, level, X, Y, b0, nr); break;
+#define ODP_WC_CASE(L) case L: cnt += run_block<(1 << L)>(st, dp, jb, level, X, Y, Mcur, b0, nr); break;
     switch(jb.wc_log2){
       ODP_WC_CASE(1) ODP_WC_CASE(2) ODP_WC_CASE(3) ODP_WC_CASE(4)
-      ODP_WC_CASE(5) ODP_WC_CASE(6) ODP_WC_CASE(7) ODP_WC_CASE(8)
+      ODP_WC_CASE(5) ODP_WC_CASE(6) ODP_WC_CASE(7)
       default: break;
     }
 #undef ODP_WC_CASE
@@ -299,10 +369,6 @@ __device__ unsigned run_rows(int *sidx, const gbx_job &jb, int level, const unsi
   }
   return cnt;
 }
-
-/* ---------------------------------------------------------------------- */
-/* Persistent engine.                                                      */
-/* ---------------------------------------------------------------------- */
 
 /* Takes one tile from the first slot (from `cursor` on) that has one left.
  * The ticket is read before it is incremented, so slots without tiles are
@@ -332,8 +398,9 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   __shared__ gbx_job sh_job;
   __shared__ int sh_state, sh_slot, sh_tile, sh_level;
   __shared__ unsigned long long *sh_buf0, *sh_buf1;
+  __shared__ unsigned *sh_mask0, *sh_mask1;
   __shared__ unsigned sh_warp[ENGINE_WARPS];
-  __shared__ __align__(16) int sh_idx[IDX_SMEM_INTS];
+  __shared__ __align__(16) Stage sh_stage;
 
   int cursor = blockIdx.x % nslots;
   unsigned long long idle_since = 0;
@@ -353,6 +420,8 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
         sh_job = jobs[vload(&sl->job)];
         sh_buf0 = vload(&sl->buf0);
         sh_buf1 = vload(&sl->buf1);
+        sh_mask0 = vload(&sl->mask0);
+        sh_mask1 = vload(&sl->mask1);
         idle_since = 0;
         /* Take the next ticket now so its round trip overlaps this tile.  Not
          * for one-tile jobs: their CTA keeps going level after level. */
@@ -385,6 +454,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
     const gbx_job jb = sh_job;
     gbx_slot *sl = &slots[sh_slot];
     unsigned long long *buf0 = sh_buf0, *buf1 = sh_buf1;
+    unsigned *mask0 = sh_mask0, *mask1 = sh_mask1;
     int level = sh_level, tile = sh_tile;
     __syncthreads();
 
@@ -392,9 +462,11 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
       /* level k writes buffer k&1 and reads buffer (k-1)&1 */
       const unsigned long long *X = (level & 1) ? buf0 : buf1;
       unsigned long long *Y = (level & 1) ? buf1 : buf0;
+      const unsigned *Mprev = (level & 1) ? mask0 : mask1;
+      unsigned *Mcur = (level & 1) ? mask1 : mask0;
       const int r0 = tile * jb.tile_rows;
       const int r1 = min(r0 + jb.tile_rows, jb.n);
-      unsigned cnt = run_rows(sh_idx, jb, level, X, Y, r0, r1);
+      unsigned cnt = run_rows(sh_stage, jb, level, X, Y, Mprev, Mcur, r0, r1);
       cnt = __reduce_add_sync(0xffffffffu, cnt);
       if((threadIdx.x & 31) == 0) sh_warp[threadIdx.x >> 5] = cnt;
       __threadfence();                                 /* release this thread's row writes */
@@ -409,7 +481,8 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
         int next = 0;
         if(old + 1 == (unsigned)jb.ntiles){           /* this CTA closes the level */
           __threadfence();
-          const unsigned long long c = vload(&sl->count);
+          /* level 1 counts bits set, later levels count bits added */
+          const unsigned long long c = (level == 1 ? 0ull : vload(&sl->prev)) + vload(&sl->count);
           const unsigned long long full = (unsigned long long)jb.n * (unsigned long long)jb.nsrc;
           const bool complete = (c == full);
           const bool stalled = !complete && (c == vload(&sl->prev) || level >= jb.n);
@@ -717,7 +790,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   while((1 << full_l2) < W) full_l2++;
 
   /* Layout of the scratch array for the widest chunk (<= 64 words) that fits. */
-  size_t off_adj = 0, off_nbr = 0, off_desc = 0, off_jobs = 0, off_state = 0, off_buf = 0, total = 0;
+  size_t off_adj = 0, off_nbr = 0, off_desc = 0, off_jobs = 0, off_state = 0, off_buf = 0, off_mask = 0, total = 0;
   size_t out_off = 0, acc_off = 0, levels_off = 0, state_bytes = 0;
   int wl = full_l2 < 6 ? full_l2 : 6, njobs = 0, nslots = 0, fits = 0;
   for(; wl >= 1; wl--){
@@ -734,7 +807,8 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
     levels_off = acc_off + 64;
     state_bytes = levels_off + sizeof(int) * (size_t)njobs;
     off_buf = up256(off_state + state_bytes);
-    total = off_buf + sizeof(unsigned long long) * 2 * (size_t)nslots * ((size_t)n << wl);
+    off_mask = up256(off_buf + sizeof(unsigned long long) * 2 * (size_t)nslots * ((size_t)n << wl));
+    total = off_mask + sizeof(unsigned) * 2 * (size_t)nslots * (size_t)n;
     if(total <= ODPX_NOALLOC_SCRATCH_BYTES){ fits = 1; break; }
   }
   if(!fits){
@@ -794,6 +868,8 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
     sl[k].sum = ((long long)n * jobs[k].nsrc - jobs[k].nsrc) * s;
     sl[k].buf0 = bufs + (size_t)k * 2 * ((size_t)n << wl);
     sl[k].buf1 = sl[k].buf0 + ((size_t)n << wl);
+    sl[k].mask0 = (unsigned *)(base + off_mask) + (size_t)k * 2 * n;
+    sl[k].mask1 = sl[k].mask0 + n;
   }
   ((gbx_ctrl *)(state + out_off))->next_job = (unsigned)nslots;
 

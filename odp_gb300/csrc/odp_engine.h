@@ -30,13 +30,14 @@ typedef struct {
 /* One (graph, column chunk) BFS job: sources [src0, src0 + nsrc). */
 typedef struct {
   const int *nbr;          /* device int[n][dp] */
+  const int *srcpos;       /* device int[n]: row -> source ordinal (-1: not a source), or NULL: row itself */
   int n, dp;
-  int wc_log2;             /* words (uint64) per row in this chunk = 1 << wc_log2, >= 1 */
-  int src0, nsrc;
+  int wc_log2;             /* words (uint64) per row in this chunk = 1 << wc_log2, 1..7 */
+  int src0, nsrc;          /* source ordinals [src0, src0 + nsrc) */
   int sym;                 /* symmetries: sums are scaled by it */
   int graph;               /* index into the graph accumulators */
   int tile_rows, ntiles;
-  int pad[3];
+  int pad;
 } gbx_job;
 
 /* Per-slot mutable state, one 128-byte line each. */
@@ -46,11 +47,12 @@ typedef struct {
   int job;                     /* job index */
   int level;                   /* BFS level being computed (>= 1) */
   int pad0;
-  unsigned long long count;    /* bits set so far at this level */
+  unsigned long long count;    /* level 1: bits set; later levels: bits added */
   unsigned long long prev;     /* bits set at the previous level */
   long long sum;               /* this job's share of the ordered distance sum */
   unsigned long long *buf0, *buf1;
-  unsigned long long pad1[8];
+  unsigned int *mask0, *mask1; /* per row: which lanes' words changed at a level */
+  unsigned long long pad1[6];
 } gbx_slot;
 
 typedef struct {

@@ -143,6 +143,31 @@ static void fill_degrees(const odp_shape *sh, int n, int *out)
   }
 }
 
+/* Source ordinals of a grid graph, ordered by square tiles of the base
+ * region (the whole grid, the left half for s = 2, the lower-left quadrant
+ * for s = 4), so that each column chunk's sources are close together and its
+ * BFS wavefront stays narrow.  Indexed by row; rows that are not sources get
+ * -1.  Any assignment of sources to bits gives the same results: the sum and
+ * the diameter do not depend on which sources share a chunk. */
+static void fill_srcpos(const odp_plan_graph *g, int *srcpos)
+{
+  int bw = g->s == 1 ? g->width : g->width / 2;
+  int bh = g->s == 4 ? g->height / 2 : g->height;
+  int cap = 64 << g->wc_log2, ts = 1;
+  while((ts + 1) * (ts + 1) <= cap) ts++;
+  for(int r = 0; r < g->n; r++) srcpos[r] = -1;
+  int ord = 0;
+  for(int tx = 0; tx < bw; tx += ts)
+    for(int ty = 0; ty < bh; ty += ts)
+      for(int x = tx; x < tx + ts && x < bw; x++)
+        for(int y = ty; y < ty + ts && y < bh; y++){
+          /* rows of base vertices: v itself for s = 1, 2 (x < w/2); the local
+           * index x * (h/2) + y for s = 4 */
+          int row = (g->s == 4) ? x * bh + y : x * g->height + y;
+          srcpos[row] = ord++;
+        }
+}
+
 typedef struct { int job; double work; } job_order;
 
 static int cmp_work_desc(const void *a, const void *b)
@@ -201,7 +226,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       wl = full_l2 < 4 ? full_l2 : 4;
     }
     if(wl < 1) wl = 1;
-    if(wl > 8) wl = 8;
+    if(wl > 7) wl = 7;                 /* rows of at most 1 KB per chunk */
     if(wl > full_l2 && full_l2 >= 1) wl = full_l2;
     g->wc_log2 = wl;
     const int wc = 1 << wl;
@@ -220,11 +245,13 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     g->ntiles = (g->n + g->tile_rows - 1) / g->tile_rows;
     g->has_ndeg = sh->num_degrees != NULL;
     g->has_itable = g->grid_s;
+    g->has_srcpos = sh->grid;             /* grids: spatially compact source chunks */
     g->adj_ints = (size_t)g->B * g->d;
     g->adj_off = p->adj_ints;       p->adj_ints += ALIGN_UP(g->adj_ints, 4);
     g->ndeg_off = p->ndeg_ints;     if(g->has_ndeg) p->ndeg_ints += ALIGN_UP((size_t)g->n, 4);
     g->itable_off = p->itable_ints; if(g->has_itable) p->itable_ints += ALIGN_UP((size_t)g->n, 4);
     g->nbr_off = p->nbr_ints;       p->nbr_ints += (size_t)g->n * g->dp;
+    g->srcpos_off = p->srcpos_ints; if(g->has_srcpos) p->srcpos_ints += ALIGN_UP((size_t)g->n, 4);
     p->total_vertices += g->n;
     njobs += g->nchunks;
   }
@@ -258,12 +285,13 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
 
   /* Slots: as many concurrent jobs as the L2 budget holds (at least 2 when
    * there are 2 jobs), capped by the job count. */
-  size_t max_words = 0;
+  size_t max_words = 0, max_rows = 0;
   double sum_fp = 0;
   int fit = 0;
   for(int k = 0; k < njobs; k++){
     size_t w = (size_t)p->h_jobs[k].n << p->h_jobs[k].wc_log2;
     if(w > max_words) max_words = w;
+    if((size_t)p->h_jobs[k].n > max_rows) max_rows = (size_t)p->h_jobs[k].n;
     double fp = 2.0 * 8.0 * (double)w;
     if(sum_fp + fp <= budget){ sum_fp += fp; fit++; }
   }
@@ -278,6 +306,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   if(nslots < 1) nslots = 1;
   p->nslots = nslots;
   p->slot_words = ALIGN_UP(max_words, 32);
+  p->slot_rows = ALIGN_UP(max_rows, 64);
 
   /* Device memory. */
   p->out_off = sizeof(gbx_slot) * (size_t)nslots;
@@ -292,6 +321,8 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   if(p->itable_ints) CK(gbx_malloc((void **)&p->d_itable, sizeof(int) * p->itable_ints));
   CK(gbx_malloc((void **)&p->d_nbr, sizeof(int) * (p->nbr_ints ? p->nbr_ints : 4)));
   CK(gbx_malloc((void **)&p->d_slotbuf, sizeof(unsigned long long) * p->slot_words * 2 * (size_t)nslots));
+  CK(gbx_malloc((void **)&p->d_slotmask, sizeof(unsigned int) * p->slot_rows * 2 * (size_t)nslots));
+  if(p->srcpos_ints) CK(gbx_malloc((void **)&p->d_srcpos, sizeof(int) * p->srcpos_ints));
   CK(gbx_malloc((void **)&p->d_expand, sizeof(gbx_expand_desc) * (size_t)count));
   CK(gbx_malloc((void **)&p->d_jobs, sizeof(gbx_job) * (size_t)njobs));
   CK(gbx_malloc((void **)&p->d_state, p->state_bytes));
@@ -303,6 +334,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   {
     int *h_nd = p->ndeg_ints ? malloc(sizeof(int) * p->ndeg_ints) : NULL;
     int *h_it = p->itable_ints ? malloc(sizeof(int) * p->itable_ints) : NULL;
+    int *h_sp = p->srcpos_ints ? malloc(sizeof(int) * p->srcpos_ints) : NULL;
     gbx_expand_desc *ed = calloc((size_t)count, sizeof(gbx_expand_desc));
     long long first = 0;
     for(int i = 0; i < count; i++){
@@ -314,6 +346,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       }
       else g->row_reads = (double)g->n * (g->d + 2);
       if(g->has_itable) fill_itable(g->width, g->height, g->s, h_it + g->itable_off);
+      if(g->has_srcpos) fill_srcpos(g, h_sp + g->srcpos_off);
       gbx_expand_desc *e = &ed[i];
       e->adj = p->d_adj + g->adj_off;
       e->ndeg = g->has_ndeg ? p->d_ndeg + g->ndeg_off : NULL;
@@ -324,13 +357,18 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       e->first_vertex = first;
       first += g->n;
     }
-    for(int k = 0; k < njobs; k++) p->h_jobs[k].nbr = p->d_nbr + p->g[p->h_jobs[k].graph].nbr_off;
+    for(int k = 0; k < njobs; k++){
+      const odp_plan_graph *g = &p->g[p->h_jobs[k].graph];
+      p->h_jobs[k].nbr = p->d_nbr + g->nbr_off;
+      p->h_jobs[k].srcpos = g->has_srcpos ? p->d_srcpos + g->srcpos_off : NULL;
+    }
+    if(h_sp) CK(gbx_memcpy_h2d(p->d_srcpos, h_sp, sizeof(int) * p->srcpos_ints, p->stream));
     if(h_nd) CK(gbx_memcpy_h2d(p->d_ndeg, h_nd, sizeof(int) * p->ndeg_ints, p->stream));
     if(h_it) CK(gbx_memcpy_h2d(p->d_itable, h_it, sizeof(int) * p->itable_ints, p->stream));
     CK(gbx_memcpy_h2d(p->d_expand, ed, sizeof(gbx_expand_desc) * (size_t)count, p->stream));
     CK(gbx_memcpy_h2d(p->d_jobs, p->h_jobs, sizeof(gbx_job) * (size_t)njobs, p->stream));
     CK(gbx_stream_sync(p->stream));
-    free(h_nd); free(h_it); free(ed);
+    free(h_nd); free(h_it); free(h_sp); free(ed);
   }
 
   /* Initial engine state: the first nslots jobs loaded into the slots. */
@@ -346,6 +384,8 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       sl[k].sum = ((long long)j->n * j->nsrc - j->nsrc) * j->sym;
       sl[k].buf0 = p->d_slotbuf + (size_t)k * 2 * p->slot_words;
       sl[k].buf1 = sl[k].buf0 + p->slot_words;
+      sl[k].mask0 = p->d_slotmask + (size_t)k * 2 * p->slot_rows;
+      sl[k].mask1 = sl[k].mask0 + p->slot_rows;
     }
     gbx_ctrl *ctrl = (gbx_ctrl *)(p->h_state_init + p->out_off);
     ctrl->next_job = (unsigned)nslots;
@@ -363,7 +403,7 @@ void odp_plan_destroy(odp_plan *p)
   if(!p) return;
   if(p->graph_exec) gbx_graph_destroy(p->graph_exec);
   gbx_free(p->d_adj); gbx_free(p->d_ndeg); gbx_free(p->d_itable); gbx_free(p->d_nbr);
-  gbx_free(p->d_slotbuf); gbx_free(p->d_expand); gbx_free(p->d_jobs); gbx_free(p->d_state);
+  gbx_free(p->d_slotbuf); gbx_free(p->d_slotmask); gbx_free(p->d_srcpos); gbx_free(p->d_expand); gbx_free(p->d_jobs); gbx_free(p->d_state);
   gbx_host_free(p->h_adj); gbx_host_free(p->h_state_init); gbx_host_free(p->h_state_out);
   if(p->stream) gbx_stream_destroy(p->stream);
   free(p->h_jobs);

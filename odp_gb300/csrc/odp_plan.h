@@ -34,9 +34,9 @@ typedef struct {
   int grid, n, d, dp, s, grid_s, width, height;
   int B, W;                    /* sources (n/s) and uint64 words per full row */
   int wc_log2, nchunks, tile_rows, ntiles;
-  size_t adj_off, ndeg_off, itable_off, nbr_off;   /* int offsets into packed arrays */
+  size_t adj_off, ndeg_off, itable_off, nbr_off, srcpos_off;   /* int offsets into packed arrays */
   size_t adj_ints;
-  int has_ndeg, has_itable;
+  int has_ndeg, has_itable, has_srcpos;
   double row_reads;            /* sum over vertices of (degree + 2): rows touched per row per level */
 } odp_plan_graph;
 
@@ -44,11 +44,12 @@ typedef struct odp_plan {
   int ngraphs, njobs, nslots;
   odp_plan_graph *g;
   odp_tuning tuning;
-  size_t adj_ints, ndeg_ints, itable_ints, nbr_ints, slot_words;
+  size_t adj_ints, ndeg_ints, itable_ints, nbr_ints, srcpos_ints, slot_words, slot_rows;
   long long total_vertices;
   /* device */
-  int *d_adj, *d_ndeg, *d_itable, *d_nbr;
+  int *d_adj, *d_ndeg, *d_itable, *d_nbr, *d_srcpos;
   unsigned long long *d_slotbuf;
+  unsigned int *d_slotmask;
   gbx_expand_desc *d_expand;
   gbx_job *d_jobs;
   char *d_state;               /* slots | ctrl | error | accumulators */

@@ -278,3 +278,35 @@ def test_grid_256x256_fixture(golden):
     edges = og.conv_adjacency2edge_grid(w, h, 6, adj)
     assert sha256(edges) == g["sha256"] == bytes(z["edges_sha256"]).decode()
     assert same(gpu_aspl(adj, grid=True, width=w, height=h), result_tuple(g["reference"]))
+
+
+@pytest.mark.parametrize("s", [1, 2, 4])
+@pytest.mark.parametrize("wc_log2", [1, 2, 4, 6])
+def test_grid_source_tiles_and_chunk_widths(s, wc_log2):
+    """Grid graphs use spatially compact source chunks; any chunk width and
+    any source order give the reference's results."""
+    w = h = 40
+    d, length = 6, 3
+    adj = og.conv_edge2adjacency_grid(w, h, og.generate_random_grid(w, h, d, length, s, seed=31 + s), d, s)
+    ref = oracle.aspl(adj, grid=True, width=w, height=h, symmetries=s)
+    og.set_tuning(wc_log2=wc_log2, slots=2, local_kb=1)
+    try:
+        b = og.Batch([og.GraphSpec(adj, grid=True, width=w, height=h, symmetries=s)])
+        assert same(b.run()[0], ref)
+        assert same(b.run()[0], ref)          # a second run on the same buffers
+        b.close()
+    finally:
+        og.set_tuning()
+
+
+def test_batch_workload_sample_against_oracle():
+    """The first graphs of the benchmark's batched workload, evaluated
+    together, against the oracle one by one."""
+    from odp_gb300 import workloads
+    shapes = workloads.batch_shapes(512)[:48]
+    specs = workloads.build_graphs(shapes)
+    got = og.set_aspl_batch(specs)
+    for sp, g in zip(specs, got):
+        o = oracle.aspl(sp.adjacency, nodes=sp.nodes, symmetries=sp.symmetries, grid=sp.grid, width=sp.width,
+                        height=sp.height)
+        assert same(g, o), (sp.nodes, sp.grid, sp.symmetries)
