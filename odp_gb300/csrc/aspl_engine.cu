@@ -206,7 +206,7 @@ __device__ __forceinline__ int source_of(const int *srcpos, int row)
 
 /* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources, and the
  * lanes of each row whose words differ from the identity P_0. */
-template <int WC>
+template <int WC, bool ACT>
 __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsigned long long *Y,
                                 unsigned *Mcur, int row0, int nrows)
 {
@@ -243,9 +243,60 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
         changed |= (acc[k].x != id[k].x) | (acc[k].y != id[k].y) | (acc[k].z != id[k].z) | (acc[k].w != id[k].w);
       }
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, changed);
-    if(valid && gl == 0)
-      Mcur[row0 + r] = S::G == 32 ? bal : (bal >> (sub * S::G)) & ((1u << S::G) - 1u);
+    if(ACT){
+      const unsigned bal = __ballot_sync(0xffffffffu, changed);
+      if(valid && gl == 0)
+        Mcur[row0 + r] = S::G == 32 ? bal : (bal >> (sub * S::G)) & ((1u << S::G) - 1u);
+    }
+  }
+  return cnt;
+}
+
+/* Level k >= 2 without change tracking: P_k[v] = P_{k-1}[v] | OR_j
+ * P_{k-1}[nbr[v][j]] over all neighbours, every word written.  Eight 16-byte
+ * loads per lane are in flight per step (NB neighbours x V vectors).
+ * Returns the bits added at this level. */
+template <int WC>
+__device__ unsigned rows_levelk_all(const Stage &st, int dp, const unsigned long long *X, unsigned long long *Y,
+                                    int row0, int nrows)
+{
+  typedef RowShape<WC> S;
+  constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / S::G, gl = lane % S::G;
+  const uint4 *Xv = reinterpret_cast<const uint4 *>(X);
+  unsigned cnt = 0;
+  for(int r = warp * S::RPW + sub; r < nrows; r += ENGINE_WARPS * S::RPW){
+    const int row = row0 + r;
+    uint4 acc[S::V];
+    const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
+    unsigned before = 0;
+#pragma unroll
+    for(int k = 0; k < S::V; k++){ acc[k] = __ldcg(xr + k * S::G); before += popc4(acc[k]); }
+    const int *ip = st.idx + r * dp;
+    for(int j = 0; j < dp; j += NB){
+      uint4 t[NB][S::V];
+#pragma unroll
+      for(int i = 0; i < NB; i++){
+        const int idx = (j + i < dp) ? ip[j + i] : -1;
+        const uint4 *nr = Xv + (size_t)(idx < 0 ? 0 : idx) * S::VPR + gl;
+#pragma unroll
+        for(int k = 0; k < S::V; k++)
+          t[i][k] = (idx >= 0) ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+      }
+#pragma unroll
+      for(int i = 0; i < NB; i++)
+#pragma unroll
+        for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
+    }
+    uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
+    unsigned after = 0;
+#pragma unroll
+    for(int k = 0; k < S::V; k++){
+      __stcg(yr + k * S::G, acc[k]);
+      after += popc4(acc[k]);
+    }
+    cnt += after - before;
   }
   return cnt;
 }
@@ -324,8 +375,11 @@ template <int WC>
 __device__ unsigned run_block(const Stage &st, int dp, const gbx_job &jb, int level, const unsigned long long *X,
                               unsigned long long *Y, unsigned *Mcur, int row0, int nrows)
 {
-  return level == 1 ? rows_level1<WC>(st, dp, jb, Y, Mcur, row0, nrows)
-                    : rows_levelk<WC>(st, dp, X, Y, Mcur, row0, nrows, level == 2);
+  if(jb.flags & GBX_JOB_ACTIVE)
+    return level == 1 ? rows_level1<WC, true>(st, dp, jb, Y, Mcur, row0, nrows)
+                      : rows_levelk<WC>(st, dp, X, Y, Mcur, row0, nrows, level == 2);
+  return level == 1 ? rows_level1<WC, false>(st, dp, jb, Y, Mcur, row0, nrows)
+                    : rows_levelk_all<WC>(st, dp, X, Y, row0, nrows);
 }
 
 /* Rows [r0, r1) of one level, block by block: stage the block's neighbour
@@ -343,7 +397,7 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
     const int4 *src = reinterpret_cast<const int4 *>(jb.nbr + (size_t)b0 * dp);
     int4 *dst = reinterpret_cast<int4 *>(st.idx);
     for(int i = threadIdx.x; i < (nr * dp) >> 2; i += ENGINE_THREADS) dst[i] = __ldg(src + i);
-    if(level > 1){
+    if(level > 1 && (jb.flags & GBX_JOB_ACTIVE)){
       for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS) st.own[r] = __ldcg(Mprev + b0 + r);
       __syncthreads();
       for(int i = threadIdx.x; i < nr * dp; i += ENGINE_THREADS){

@@ -37,8 +37,10 @@ typedef struct {
   int sym;                 /* symmetries: sums are scaled by it */
   int graph;               /* index into the graph accumulators */
   int tile_rows, ntiles;
-  int pad;
+  int flags;               /* GBX_JOB_ACTIVE: gather only words that changed at the previous level */
 } gbx_job;
+
+#define GBX_JOB_ACTIVE 1
 
 /* Per-slot mutable state, one 128-byte line each. */
 typedef struct {

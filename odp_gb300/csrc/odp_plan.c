@@ -49,6 +49,7 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->local_kb = env_int("ODP_GB300_LOCAL_KB", batch ? 2048 : 96);
   t->use_graph = env_int("ODP_GB300_GRAPH", 1);
   t->blocks = env_int("ODP_GB300_BLOCKS", 0);
+  t->activity = env_int("ODP_GB300_ACTIVITY", -1);
 }
 
 static int ilog2_ceil(long long x)
@@ -272,6 +273,11 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
         j->nsrc = g->B - j->src0 < wc * 64 ? g->B - j->src0 : wc * 64;
         j->sym = g->s; j->graph = i;
         j->tile_rows = g->tile_rows; j->ntiles = g->ntiles;
+        /* Grids have long, narrow BFS wavefronts: most words stop changing
+         * long before the last level, so only changed words are gathered.
+         * Random graphs change almost every word at almost every level. */
+        int act = tuning->activity < 0 ? g->grid : tuning->activity;
+        j->flags = act ? GBX_JOB_ACTIVE : 0;
         ord[k].job = k;
         ord[k].work = (double)g->n * wc * (g->d + 2) * (count > 1 ? 1.0 : 0.0);
       }
@@ -298,7 +304,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   int nslots = tuning->slots > 0 ? tuning->slots : fit;
   if(tuning->slots <= 0){
     if(nslots < 2) nslots = 2;
-    if(count == 1 && nslots > 4) nslots = 4;
+    /* a single grid graph runs many levels with little work each: keep more
+     * chunks in flight (its active working set is a narrow band) */
+    if(count == 1 && p->h_jobs[0].flags & GBX_JOB_ACTIVE) nslots = 32;
+    else if(count == 1 && nslots > 4) nslots = 4;
     if(count > 1 && nslots < 32) nslots = 32;
     if(nslots > 512) nslots = 512;
   }

@@ -310,3 +310,34 @@ def test_batch_workload_sample_against_oracle():
         o = oracle.aspl(sp.adjacency, nodes=sp.nodes, symmetries=sp.symmetries, grid=sp.grid, width=sp.width,
                         height=sp.height)
         assert same(g, o), (sp.nodes, sp.grid, sp.symmetries)
+
+
+@pytest.mark.parametrize("activity", ["0", "1"])
+def test_change_tracking_on_and_off(golden, activity, monkeypatch):
+    """Both level passes (all neighbours / only neighbours whose words
+    changed) on general graphs, grids and the golden edge cases."""
+    monkeypatch.setenv("ODP_GB300_ACTIVITY", activity)
+    rng = np.random.default_rng(99)
+    specs, kws = [], []
+    for _ in range(20):
+        spec, kw = random_graph(rng)
+        specs.append(spec)
+        kws.append(kw)
+    for c in golden["cases"]:
+        if c["kind"] == "general":
+            specs.append(og.GraphSpec(case_adjacency(c), nodes=c["nodes"], symmetries=c["symmetries"],
+                                      num_degrees=case_degrees(c)))
+            kws.append(dict(nodes=c["nodes"], symmetries=c["symmetries"], num_degrees=case_degrees(c)))
+    b = og.Batch(specs)
+    for g, spec, kw in zip(b.run(), specs, kws):
+        assert same(g, oracle.aspl(spec.adjacency, **kw)), kw
+    b.close()
+    n, d = 4096, 10
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=4), d)
+    og.set_tuning(wc_log2=3, slots=3, local_kb=1)
+    try:
+        b = og.Batch([og.GraphSpec(adj, nodes=n)])
+        assert same(b.run()[0], oracle.aspl(adj, nodes=n))
+        b.close()
+    finally:
+        og.set_tuning()
