@@ -454,7 +454,10 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   __shared__ unsigned long long *sh_buf0, *sh_buf1;
   __shared__ unsigned *sh_mask0, *sh_mask1;
   __shared__ unsigned sh_warp[ENGINE_WARPS];
-  __shared__ __align__(16) Stage sh_stage;
+  /* Staging area in dynamic shared memory: the launch gives the whole Stage
+   * when some job tracks changes, else only its index block. */
+  extern __shared__ __align__(16) unsigned char dyn_smem[];
+  Stage &sh_stage = *reinterpret_cast<Stage *>(dyn_smem);
 
   int cursor = blockIdx.x % nslots;
   unsigned long long idle_since = 0;
@@ -604,7 +607,10 @@ __global__ void __launch_bounds__(256) l2_read_probe_kernel(const uint4 *__restr
   if((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9e3779b9u) sink[0] = 1;   /* keeps the loads */
 }
 
-int g_engine_blocks = 0;
+int g_engine_blocks = 0, g_engine_blocks_active = 0;
+
+constexpr size_t STAGE_BYTES_PLAIN = sizeof(int) * IDX_SMEM_INTS;
+constexpr size_t STAGE_BYTES_ACTIVE = sizeof(Stage);
 
 }  // namespace
 
@@ -626,16 +632,19 @@ int gbx_device_init(int *sm_count)
   if(e != cudaSuccess) return (int)e;
   if(sm_count) *sm_count = sms;
   if(g_engine_blocks == 0){
-    int per_sm = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, 0);
+    int per_sm = 0, per_sm_active = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, STAGE_BYTES_PLAIN);
     if(e != cudaSuccess) return (int)e;
-    if(per_sm < 1) per_sm = 1;
-    g_engine_blocks = per_sm * sms;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_active, engine_kernel, ENGINE_THREADS,
+                                                      STAGE_BYTES_ACTIVE);
+    if(e != cudaSuccess) return (int)e;
+    g_engine_blocks = (per_sm < 1 ? 1 : per_sm) * sms;
+    g_engine_blocks_active = (per_sm_active < 1 ? 1 : per_sm_active) * sms;
   }
   return 0;
 }
 
-int gbx_engine_blocks(void) { return g_engine_blocks; }
+int gbx_engine_blocks(int active) { return active ? g_engine_blocks_active : g_engine_blocks; }
 
 int gbx_l2_read_probe(size_t bytes, int reps, double *gbs)
 {
@@ -712,12 +721,14 @@ int gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertic
 
 int gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots, gbx_ctrl *d_ctrl,
                       gbx_graph_acc *d_acc, int *d_job_levels, unsigned long long spin_limit_ns, int blocks,
-                      void *stream)
+                      int active, void *stream)
 {
   if(njobs <= 0 || nslots <= 0) return 0;
-  if(blocks <= 0) blocks = g_engine_blocks > 0 ? g_engine_blocks : 1;
-  engine_kernel<<<blocks, ENGINE_THREADS, 0, (cudaStream_t)stream>>>(d_jobs, njobs, d_slots, nslots, d_ctrl,
-                                                                     d_acc, d_job_levels, spin_limit_ns);
+  if(blocks <= 0) blocks = gbx_engine_blocks(active);
+  if(blocks <= 0) blocks = 1;
+  engine_kernel<<<blocks, ENGINE_THREADS, active ? STAGE_BYTES_ACTIVE : STAGE_BYTES_PLAIN,
+                  (cudaStream_t)stream>>>(d_jobs, njobs, d_slots, nslots, d_ctrl, d_acc, d_job_levels,
+                                          spin_limit_ns);
   return (int)cudaGetLastError();
 }
 
@@ -818,7 +829,8 @@ int noalloc_device(NoallocDevice **out)
     if(cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return ODPX_ERR_CUDA;
     int sms = 0, per_sm = 0;
     if(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ODPX_ERR_CUDA;
-    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, 0) != cudaSuccess)
+    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, STAGE_BYTES_PLAIN) !=
+       cudaSuccess)
       return ODPX_ERR_CUDA;
     nd->scratch = (unsigned char *)p;
     nd->blocks = (per_sm < 1 ? 1 : per_sm) * sms;
@@ -936,7 +948,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   long long eblocks = ((long long)n + 255) / 256;
   if(eblocks > 65535LL * 8) eblocks = 65535LL * 8;
   expand_kernel<<<(unsigned)eblocks, 256, 0, st>>>((const gbx_expand_desc *)(base + off_desc), 1, n, d_err);
-  engine_kernel<<<nd->blocks, ENGINE_THREADS, 0, st>>>(
+  engine_kernel<<<nd->blocks, ENGINE_THREADS, STAGE_BYTES_PLAIN, st>>>(
       (const gbx_job *)(base + off_jobs), njobs, (gbx_slot *)(base + off_state), nslots,
       (gbx_ctrl *)(base + off_state + out_off), (gbx_graph_acc *)(base + off_state + acc_off),
       (int *)(base + off_state + levels_off), 60ull * 1000000000ull);

@@ -92,12 +92,12 @@ const char *gbx_error_string(int err);
 /* Kernels. */
 int  gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices,
                 unsigned int *d_error, void *stream);
-int  gbx_engine_blocks(void);          /* persistent grid size (SMs x resident CTAs) */
+int  gbx_engine_blocks(int active);    /* persistent grid size (SMs x resident CTAs) for the launch's staging size */
 /* Streaming read bandwidth of an L2-resident buffer of `bytes` (GB/s). */
 int  gbx_l2_read_probe(size_t bytes, int reps, double *gbs);
 int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots,
                        gbx_ctrl *d_ctrl, gbx_graph_acc *d_acc, int *d_job_levels,
-                       unsigned long long spin_limit_ns, int blocks, void *stream);
+                       unsigned long long spin_limit_ns, int blocks, int active, void *stream);
 
 /* CUDA graphs: capture everything issued on `stream` between begin and end. */
 int  gbx_capture_begin(void *stream);

@@ -196,7 +196,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   p->tuning = *tuning;
   p->ngraphs = count;
   p->g = calloc((size_t)count, sizeof(odp_plan_graph));
-  p->blocks = tuning->blocks > 0 ? tuning->blocks : gbx_engine_blocks();
+  p->blocks = tuning->blocks;          /* 0: chosen per launch from the staging size */
   p->spin_limit_ns = 60ull * 1000000000ull;
   const double budget = (double)tuning->l2_budget_mb * 1024.0 * 1024.0;
   const double local_bytes = (double)tuning->local_kb * 1024.0;
@@ -285,7 +285,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   }
   qsort(ord, (size_t)njobs, sizeof(job_order), cmp_work_desc);
   p->h_jobs = calloc((size_t)njobs, sizeof(gbx_job));
-  for(int k = 0; k < njobs; k++) p->h_jobs[k] = jobs[ord[k].job];
+  for(int k = 0; k < njobs; k++){
+    p->h_jobs[k] = jobs[ord[k].job];
+    if(p->h_jobs[k].flags & GBX_JOB_ACTIVE) p->any_active = 1;
+  }
   free(jobs);
   free(ord);
 
@@ -436,7 +439,8 @@ int odp_plan_enqueue_engine(odp_plan *p)
 {
   return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
                            (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),
-                           (int *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->stream);
+                           (int *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->any_active,
+                           p->stream);
 }
 
 const int *odp_plan_job_levels(const odp_plan *p)

@@ -63,6 +63,7 @@ typedef struct odp_plan {
   void *stream, *graph_exec;
   unsigned long long spin_limit_ns;
   int blocks;
+  int any_active;              /* some job tracks changes: launch with the full staging area */
   double bytes_alg_last;       /* algorithmic bytes of the last run (roofline) */
 } odp_plan;
 
