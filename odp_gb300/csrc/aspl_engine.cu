@@ -197,16 +197,18 @@ struct Stage {
   unsigned act[BLOCK_ROWS_MAX];
 };
 
-/* Source ordinal of a row (the bit it owns across the chunks). */
+/* Source ordinal of a row (the bit it owns across the chunks): the row
+ * itself, or from the graph's source table (SP). */
+template <bool SP>
 __device__ __forceinline__ int source_of(const int *srcpos, int row)
 {
-  if(row < 0) return -1;
-  return srcpos ? __ldg(srcpos + row) : row;
+  if(!SP) return row;
+  return row < 0 ? -1 : __ldg(srcpos + row);
 }
 
 /* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources, and the
  * lanes of each row whose words differ from the identity P_0. */
-template <int WC, bool ACT>
+template <int WC, bool ACT, bool SP>
 __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsigned long long *Y,
                                 unsigned *Mcur, int row0, int nrows)
 {
@@ -224,23 +226,25 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
       uint4 acc[S::V], id[S::V];
 #pragma unroll
       for(int k = 0; k < S::V; k++){ acc[k] = make_uint4(0u, 0u, 0u, 0u); id[k] = acc[k]; }
-      const int self = source_of(jb.srcpos, row) - src0;
+      const int self = source_of<SP>(jb.srcpos, row) - src0;
       mark_source<WC>(acc, self, nsrc, gl);
-      mark_source<WC>(id, self, nsrc, gl);
+      if(ACT) mark_source<WC>(id, self, nsrc, gl);
       const int4 *ip = reinterpret_cast<const int4 *>(st.idx + r * dp);
       for(int j = 0; j < (dp >> 2); j++){
         int4 q = ip[j];
-        mark_source<WC>(acc, source_of(jb.srcpos, q.x) - src0, nsrc, gl);
-        mark_source<WC>(acc, source_of(jb.srcpos, q.y) - src0, nsrc, gl);
-        mark_source<WC>(acc, source_of(jb.srcpos, q.z) - src0, nsrc, gl);
-        mark_source<WC>(acc, source_of(jb.srcpos, q.w) - src0, nsrc, gl);
+        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.x) - src0, nsrc, gl);
+        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.y) - src0, nsrc, gl);
+        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.z) - src0, nsrc, gl);
+        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.w) - src0, nsrc, gl);
       }
       uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
 #pragma unroll
       for(int k = 0; k < S::V; k++){
         __stcg(yr + k * S::G, acc[k]);
         cnt += popc4(acc[k]);
-        changed |= (acc[k].x != id[k].x) | (acc[k].y != id[k].y) | (acc[k].z != id[k].z) | (acc[k].w != id[k].w);
+        if(ACT)
+          changed |= (acc[k].x != id[k].x) | (acc[k].y != id[k].y) | (acc[k].z != id[k].z) |
+                     (acc[k].w != id[k].w);
       }
     }
     if(ACT){
@@ -255,7 +259,7 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
 /* Level k >= 2 without change tracking: P_k[v] = P_{k-1}[v] | OR_j
  * P_{k-1}[nbr[v][j]] over all neighbours, every word written.  Eight 16-byte
  * loads per lane are in flight per step (NB neighbours x V vectors).
- * Returns the bits added at this level. */
+ * Returns the bits set at this level. */
 template <int WC>
 __device__ unsigned rows_levelk_all(const Stage &st, int dp, const unsigned long long *X, unsigned long long *Y,
                                     int row0, int nrows)
@@ -270,9 +274,8 @@ __device__ unsigned rows_levelk_all(const Stage &st, int dp, const unsigned long
     const int row = row0 + r;
     uint4 acc[S::V];
     const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
-    unsigned before = 0;
 #pragma unroll
-    for(int k = 0; k < S::V; k++){ acc[k] = __ldcg(xr + k * S::G); before += popc4(acc[k]); }
+    for(int k = 0; k < S::V; k++) acc[k] = __ldcg(xr + k * S::G);
     const int *ip = st.idx + r * dp;
     for(int j = 0; j < dp; j += NB){
       uint4 t[NB][S::V];
@@ -290,13 +293,11 @@ __device__ unsigned rows_levelk_all(const Stage &st, int dp, const unsigned long
         for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
     }
     uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
-    unsigned after = 0;
 #pragma unroll
     for(int k = 0; k < S::V; k++){
       __stcg(yr + k * S::G, acc[k]);
-      after += popc4(acc[k]);
+      cnt += popc4(acc[k]);
     }
-    cnt += after - before;
   }
   return cnt;
 }
@@ -324,12 +325,10 @@ __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long lon
     if(valid && (write_all || ((st.act[r] >> gl) & 1u))){
       const int row = row0 + r;
       const bool own = (st.own[r] >> gl) & 1u;
-      uint4 acc[S::V];
+      uint4 acc[S::V], old[S::V];
       const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
-      unsigned before = 0;
 #pragma unroll
-      for(int k = 0; k < S::V; k++){ acc[k] = __ldcg(xr + k * S::G); before += popc4(acc[k]); }
-      unsigned fresh = 0;                              /* any bit new at this level */
+      for(int k = 0; k < S::V; k++){ old[k] = __ldcg(xr + k * S::G); acc[k] = old[k]; }
       const int *ip = st.idx + r * dp;
       const unsigned *mp = st.nmask + r * dp;
       for(int j = 0; j < dp; j += NB){
@@ -346,17 +345,15 @@ __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long lon
 #pragma unroll
         for(int i = 0; i < NB; i++)
 #pragma unroll
-          for(int k = 0; k < S::V; k++){
-            fresh |= (t[i][k].x & ~acc[k].x) | (t[i][k].y & ~acc[k].y) | (t[i][k].z & ~acc[k].z) |
-                     (t[i][k].w & ~acc[k].w);
-            or_into(acc[k], t[i][k]);
-          }
+          for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
       }
-      unsigned after = 0;
+      unsigned added = 0;
 #pragma unroll
-      for(int k = 0; k < S::V; k++) after += popc4(acc[k]);
-      const unsigned added = after - before;
-      changed = fresh != 0;
+      for(int k = 0; k < S::V; k++){
+        added += popc4(acc[k]) - popc4(old[k]);
+        changed |= (acc[k].x != old[k].x) | (acc[k].y != old[k].y) | (acc[k].z != old[k].z) |
+                   (acc[k].w != old[k].w);
+      }
       if(own || changed || write_all){
         uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
 #pragma unroll
@@ -375,11 +372,14 @@ template <int WC>
 __device__ unsigned run_block(const Stage &st, int dp, const gbx_job &jb, int level, const unsigned long long *X,
                               unsigned long long *Y, unsigned *Mcur, int row0, int nrows)
 {
-  if(jb.flags & GBX_JOB_ACTIVE)
-    return level == 1 ? rows_level1<WC, true>(st, dp, jb, Y, Mcur, row0, nrows)
-                      : rows_levelk<WC>(st, dp, X, Y, Mcur, row0, nrows, level == 2);
-  return level == 1 ? rows_level1<WC, false>(st, dp, jb, Y, Mcur, row0, nrows)
-                    : rows_levelk_all<WC>(st, dp, X, Y, row0, nrows);
+  if(jb.flags & GBX_JOB_ACTIVE){
+    if(level > 1) return rows_levelk<WC>(st, dp, X, Y, Mcur, row0, nrows, level == 2);
+    return jb.srcpos ? rows_level1<WC, true, true>(st, dp, jb, Y, Mcur, row0, nrows)
+                     : rows_level1<WC, true, false>(st, dp, jb, Y, Mcur, row0, nrows);
+  }
+  if(level > 1) return rows_levelk_all<WC>(st, dp, X, Y, row0, nrows);
+  return jb.srcpos ? rows_level1<WC, false, true>(st, dp, jb, Y, Mcur, row0, nrows)
+                   : rows_level1<WC, false, false>(st, dp, jb, Y, Mcur, row0, nrows);
 }
 
 /* Rows [r0, r1) of one level, block by block: stage the block's neighbour
@@ -538,8 +538,10 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
         int next = 0;
         if(old + 1 == (unsigned)jb.ntiles){           /* this CTA closes the level */
           __threadfence();
-          /* level 1 counts bits set, later levels count bits added */
-          const unsigned long long c = (level == 1 ? 0ull : vload(&sl->prev)) + vload(&sl->count);
+          /* level 1 and the full-gather pass count bits set; the pass with
+           * change tracking counts bits added */
+          const bool delta = level > 1 && (jb.flags & GBX_JOB_ACTIVE);
+          const unsigned long long c = (delta ? vload(&sl->prev) : 0ull) + vload(&sl->count);
           const unsigned long long full = (unsigned long long)jb.n * (unsigned long long)jb.nsrc;
           const bool complete = (c == full);
           const bool stalled = !complete && (c == vload(&sl->prev) || level >= jb.n);

@@ -49,7 +49,7 @@ typedef struct {
   int job;                     /* job index */
   int level;                   /* BFS level being computed (>= 1) */
   int pad0;
-  unsigned long long count;    /* level 1: bits set; later levels: bits added */
+  unsigned long long count;    /* bits set at this level (with change tracking after level 1: bits added) */
   unsigned long long prev;     /* bits set at the previous level */
   long long sum;               /* this job's share of the ordered distance sum */
   unsigned long long *buf0, *buf1;

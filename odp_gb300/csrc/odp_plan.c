@@ -49,7 +49,7 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->local_kb = env_int("ODP_GB300_LOCAL_KB", batch ? 2048 : 96);
   t->use_graph = env_int("ODP_GB300_GRAPH", 1);
   t->blocks = env_int("ODP_GB300_BLOCKS", 0);
-  t->activity = env_int("ODP_GB300_ACTIVITY", -1);
+  t->activity = env_int("ODP_GB300_ACTIVITY", 0);
 }
 
 static int ilog2_ceil(long long x)
@@ -219,11 +219,15 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     int full_l2 = ilog2_ceil(g->W < 2 ? 2 : g->W);
     int wl;
     if(tuning->wc_log2 > 0) wl = tuning->wc_log2;
+    else if(count > 1){
+      /* batch: 256-byte rows, 64 concurrent jobs (measured best on GB300 for
+       * the 512-graph workload) */
+      wl = full_l2 < 5 ? full_l2 : 5;
+    }
     else{
       /* 128-byte rows (16 words): measured on GB300 to beat wider rows at
        * equal L2 footprint, because more chunks can be in flight (several
-       * slots) and their level boundaries overlap; in a batch it also keeps
-       * every job's working set at or below 2 MB for n <= 8192 */
+       * slots) and their level boundaries overlap */
       wl = full_l2 < 4 ? full_l2 : 4;
     }
     if(wl < 1) wl = 1;
@@ -273,9 +277,9 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
         j->nsrc = g->B - j->src0 < wc * 64 ? g->B - j->src0 : wc * 64;
         j->sym = g->s; j->graph = i;
         j->tile_rows = g->tile_rows; j->ntiles = g->ntiles;
-        /* Grids have long, narrow BFS wavefronts: most words stop changing
-         * long before the last level, so only changed words are gathered.
-         * Random graphs change almost every word at almost every level. */
+        /* Change tracking (gather only words that changed at the previous
+         * level) is exact for every graph; on GB300 its per-row staging costs
+         * about what it saves at these degrees, so it is off unless asked. */
         int act = tuning->activity < 0 ? g->grid : tuning->activity;
         j->flags = act ? GBX_JOB_ACTIVE : 0;
         ord[k].job = k;
@@ -307,11 +311,11 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   int nslots = tuning->slots > 0 ? tuning->slots : fit;
   if(tuning->slots <= 0){
     if(nslots < 2) nslots = 2;
-    /* a single grid graph runs many levels with little work each: keep more
-     * chunks in flight (its active working set is a narrow band) */
-    if(count == 1 && p->h_jobs[0].flags & GBX_JOB_ACTIVE) nslots = 32;
+    /* a single grid graph runs many levels with little work each: more
+     * chunks in flight hide the per-level hand-offs */
+    if(count == 1 && shapes[0].grid) nslots = 32;
     else if(count == 1 && nslots > 4) nslots = 4;
-    if(count > 1 && nslots < 32) nslots = 32;
+    if(count > 1 && nslots < 64) nslots = 64;
     if(nslots > 512) nslots = 512;
   }
   if(nslots > njobs) nslots = njobs;

@@ -28,7 +28,7 @@ typedef struct {
   int local_kb;                /* per-level traffic at or below which a job runs in one CTA */
   int use_graph;               /* replay through a CUDA graph */
   int blocks;                  /* persistent grid size; 0 = SMs x occupancy */
-  int activity;                /* change tracking: -1 grids only (default), 0 never, 1 always */
+  int activity;                /* change tracking: 0 never (default), 1 always, -1 grids only */
 } odp_tuning;
 
 typedef struct {
