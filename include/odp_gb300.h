@@ -29,6 +29,7 @@ extern "C" {
 #define ODPX_ERR_TIMEOUT   4   /* a device-side wait ran past its limit */
 #define ODPX_ERR_MEMORY    5   /* admission refused: over the memory budget */
 #define ODPX_ERR_STATE     6   /* call out of order (e.g. no plan) */
+#define ODPX_PENDING       7   /* ODPX_Serve_poll: not finished yet */
 
 /* One graph of a batch: the arguments of the matching ODP_Init_aspl_* call
  * plus the adjacency of ODP_Set_aspl. */
@@ -113,6 +114,43 @@ void   ODPX_Mutate_adjacency_general_s_rng(void *rng_state, int nodes, int degre
 #define ODPX_NOALLOC_SCRATCH_BYTES (16u << 20)
 int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, const int *adjacency,
                           int *diameter, long *sum, double *ASPL);
+
+/* ---- Serving: device-resident graphs, in-place 2-opt deltas, continuous
+ * batching (ODPX_Serve_*).  No counterpart in the reference. ---- */
+
+/* One compact-adjacency update, adjacency[row][slot] = value (row < n/s). */
+typedef struct { int row, slot, value; } ODPX_Delta;
+
+typedef struct {
+  int lanes;                 /* concurrent batches on the GPU (streams); default 4 */
+  int max_batch;             /* requests per batch; default 16 */
+  int max_nodes;             /* largest graph admitted; sizes the bitset slots; default 32768 */
+  int memory_mb;             /* device memory for bitset slots, all lanes; default 1024 */
+  int wc_log2;               /* column chunk width, log2 of 64-bit words; default 4 */
+} ODPX_Serve_config;
+
+typedef struct {
+  long long requests_done, batches, batched_requests;
+  int max_batch, max_inflight_lanes, slots_per_lane, blocks_per_lane;
+} ODPX_Serve_counters;
+
+typedef struct odp_server ODPX_Server;
+int  ODPX_Serve_create(const ODPX_Serve_config *config, ODPX_Server **server);
+/* Uploads a graph (the adjacency stays on the GPU); *handle names it. */
+int  ODPX_Serve_register(ODPX_Server *server, const ODP_Graph *graph, int *handle);
+/* Queues an evaluation of graph `handle` after applying `ndelta` updates to
+ * its resident adjacency (they persist).  Returns at once with a request id. */
+int  ODPX_Serve_submit(ODPX_Server *server, int handle, int ndelta, const ODPX_Delta *deltas, long long *request);
+/* Blocks until the request is done; latency_s = submit -> result. */
+int  ODPX_Serve_wait(ODPX_Server *server, long long request, int *diameter, long *sum, double *ASPL,
+                     double *latency_s);
+/* ODPX_PENDING while the request runs, else as ODPX_Serve_wait. */
+int  ODPX_Serve_poll(ODPX_Server *server, long long request, int *diameter, long *sum, double *ASPL,
+                     double *latency_s);
+int  ODPX_Serve_stats(ODPX_Server *server, ODPX_Serve_counters *stats);
+/* Copies the graph's resident adjacency back to the host (checkpoint). */
+int  ODPX_Serve_adjacency(ODPX_Server *server, int handle, int *adjacency);
+void ODPX_Serve_destroy(ODPX_Server *server);
 
 /* Library version string. */
 const char *ODPX_Version(void);

@@ -430,3 +430,130 @@ def version():
 def measure_l2_read_gbs(megabytes=48, reps=50):
     """Read bandwidth (GB/s) of an L2-resident stream: the L2 roofline ceiling."""
     return float(load().ODPX_Measure_l2_read_gbs(megabytes, reps))
+
+
+# --------------------------------------------------------------------------
+# Serving API (odp_gb300.h ODPX_Serve_*).
+# --------------------------------------------------------------------------
+
+PENDING = 7
+
+
+class Delta(ctypes.Structure):
+    """ODPX_Delta: adjacency[row][slot] = value (compact adjacency)."""
+    _fields_ = [("row", ctypes.c_int), ("slot", ctypes.c_int), ("value", ctypes.c_int)]
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("lanes", ctypes.c_int), ("max_batch", ctypes.c_int), ("max_nodes", ctypes.c_int),
+                ("memory_mb", ctypes.c_int), ("wc_log2", ctypes.c_int)]
+
+
+class ServeCounters(ctypes.Structure):
+    _fields_ = [("requests_done", ctypes.c_longlong), ("batches", ctypes.c_longlong),
+                ("batched_requests", ctypes.c_longlong), ("max_batch", ctypes.c_int),
+                ("max_inflight_lanes", ctypes.c_int), ("slots_per_lane", ctypes.c_int),
+                ("blocks_per_lane", ctypes.c_int)]
+
+
+def _bind_serve(lib):
+    if getattr(lib, "_serve_bound", False):
+        return lib
+    P, I = ctypes.c_void_p, ctypes.c_int
+    out4 = [ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_long), ctypes.POINTER(ctypes.c_double),
+            ctypes.POINTER(ctypes.c_double)]
+    sig = {
+        "ODPX_Serve_create": (I, [ctypes.POINTER(ServeConfig), ctypes.POINTER(P)]),
+        "ODPX_Serve_register": (I, [P, ctypes.POINTER(Graph), ctypes.POINTER(I)]),
+        "ODPX_Serve_submit": (I, [P, I, I, ctypes.POINTER(Delta), ctypes.POINTER(ctypes.c_longlong)]),
+        "ODPX_Serve_wait": (I, [P, ctypes.c_longlong] + out4),
+        "ODPX_Serve_poll": (I, [P, ctypes.c_longlong] + out4),
+        "ODPX_Serve_stats": (I, [P, ctypes.POINTER(ServeCounters)]),
+        "ODPX_Serve_adjacency": (I, [P, I, P]),
+        "ODPX_Serve_destroy": (None, [P]),
+    }
+    for name, (res, args) in sig.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    lib._serve_bound = True
+    return lib
+
+
+class Server:
+    """A serving instance: resident graphs, in-place 2-opt deltas, continuous
+    batching over `lanes` concurrent GPU streams."""
+
+    def __init__(self, lanes=4, max_batch=16, max_nodes=32768, memory_mb=1024, wc_log2=4):
+        lib = _bind_serve(load())
+        cfg = ServeConfig(lanes, max_batch, max_nodes, memory_mb, wc_log2)
+        h = ctypes.c_void_p()
+        _check(lib.ODPX_Serve_create(ctypes.byref(cfg), ctypes.byref(h)), "ODPX_Serve_create")
+        self._h = h
+        self._specs = {}
+
+    def register(self, spec):
+        g = spec.to_c()
+        handle = ctypes.c_int()
+        _check(load().ODPX_Serve_register(self._h, ctypes.byref(g), ctypes.byref(handle)), "ODPX_Serve_register")
+        self._specs[handle.value] = spec
+        return handle.value
+
+    def submit(self, handle, deltas=()):
+        n = len(deltas)
+        arr = (Delta * max(n, 1))(*[Delta(int(r), int(s), int(v)) for r, s, v in deltas])
+        rid = ctypes.c_longlong()
+        _check(load().ODPX_Serve_submit(self._h, handle, n, arr, ctypes.byref(rid)), "ODPX_Serve_submit")
+        return rid.value
+
+    def _out(self, fn, rid):
+        d, s, a, lat = ctypes.c_int(), ctypes.c_long(), ctypes.c_double(), ctypes.c_double()
+        rc = fn(self._h, rid, ctypes.byref(d), ctypes.byref(s), ctypes.byref(a), ctypes.byref(lat))
+        return rc, (d.value, s.value, a.value, lat.value)
+
+    def wait(self, rid):
+        """(diameter, sum, ASPL, latency_s) of a request, blocking."""
+        rc, out = self._out(load().ODPX_Serve_wait, rid)
+        _check(rc, "ODPX_Serve_wait")
+        return out
+
+    def poll(self, rid):
+        rc, out = self._out(load().ODPX_Serve_poll, rid)
+        if rc == PENDING:
+            return None
+        _check(rc, "ODPX_Serve_poll")
+        return out
+
+    def stats(self):
+        c = ServeCounters()
+        _check(load().ODPX_Serve_stats(self._h, ctypes.byref(c)), "ODPX_Serve_stats")
+        return {f: getattr(c, f) for f, _ in ServeCounters._fields_}
+
+    def adjacency(self, handle):
+        spec = self._specs[handle]
+        out = np.zeros_like(spec.adjacency)
+        _check(load().ODPX_Serve_adjacency(self._h, handle, out.ctypes.data), "ODPX_Serve_adjacency")
+        return out
+
+    def close(self):
+        if self._h:
+            load().ODPX_Serve_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def two_opt_deltas(adjacency, restore, nodes, symmetries=1):
+    """The compact-adjacency slots a 2-opt swap (its ODP_Restore record)
+    touched, with their current values: what a served graph must apply."""
+    base = nodes // symmetries
+    out = []
+    for i in range(2):
+        for vert, slot in ((restore.u[i], restore.u_d[i]), (restore.v[i], restore.v_d[i])):
+            row = vert % base
+            out.append((row, slot, int(adjacency[row, slot])))
+    return out

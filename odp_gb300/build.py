@@ -62,7 +62,7 @@ def build(verbose_ptxas=False):
         logs = list(ex.map(lambda s: _compile(s, verbose_ptxas), sources))
     objs = [_obj(s) for s in sources]
     tmp_so = SO_PATH + ".tmp"
-    _run([NVCC, ARCH, "-shared", "-cudart", "static", "-o", tmp_so] + objs + ["-lm"])
+    _run([NVCC, ARCH, "-shared", "-cudart", "static", "-o", tmp_so] + objs + ["-lm", "-lpthread"])
     os.replace(tmp_so, SO_PATH)
     if os.path.exists(A_PATH):
         os.remove(A_PATH)

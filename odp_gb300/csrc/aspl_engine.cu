@@ -609,6 +609,14 @@ __global__ void __launch_bounds__(256) l2_read_probe_kernel(const uint4 *__restr
   if((acc.x ^ acc.y ^ acc.z ^ acc.w) == 0x9e3779b9u) sink[0] = 1;   /* keeps the loads */
 }
 
+/* Applies (address, value) int writes: the in-place 2-opt updates of a
+ * served graph's adjacency and neighbour table, in stream order before the
+ * evaluation that must see them. */
+__global__ void scatter_kernel(const gbx_write *__restrict__ w, int count)
+{
+  for(int i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) *w[i].at = w[i].value;
+}
+
 int g_engine_blocks = 0, g_engine_blocks_active = 0;
 
 constexpr size_t STAGE_BYTES_PLAIN = sizeof(int) * IDX_SMEM_INTS;
@@ -734,6 +742,15 @@ int gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int n
   return (int)cudaGetLastError();
 }
 
+int gbx_scatter(const gbx_write *d_writes, int count, void *stream)
+{
+  if(count <= 0) return 0;
+  int blocks = (count + 255) / 256;
+  if(blocks > 1024) blocks = 1024;
+  scatter_kernel<<<blocks, 256, 0, (cudaStream_t)stream>>>(d_writes, count);
+  return (int)cudaGetLastError();
+}
+
 int gbx_capture_begin(void *stream)
 {
   return (int)cudaStreamBeginCapture((cudaStream_t)stream, cudaStreamCaptureModeThreadLocal);
@@ -771,6 +788,14 @@ int gbx_event_create(void **ev)
 }
 
 int gbx_event_destroy(void *ev) { return (int)cudaEventDestroy((cudaEvent_t)ev); }
+
+int gbx_event_query(void *ev)
+{
+  cudaError_t e = cudaEventQuery((cudaEvent_t)ev);
+  if(e == cudaSuccess) return 0;
+  if(e == cudaErrorNotReady){ cudaGetLastError(); return 1; }
+  return (int)e;
+}
 int gbx_event_record(void *ev, void *stream) { return (int)cudaEventRecord((cudaEvent_t)ev, (cudaStream_t)stream); }
 
 int gbx_event_elapsed_ms(void *start, void *stop, float *ms)

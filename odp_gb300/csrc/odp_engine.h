@@ -72,6 +72,13 @@ typedef struct {
   int flags;                   /* 1: some chunk stalled (disconnected) */
 } gbx_graph_acc;
 
+/* One int write into device memory (served-graph updates). */
+typedef struct {
+  int *at;
+  int value;
+  int pad;
+} gbx_write;
+
 #define GBX_ERR_BAD_ADJ   1u   /* adjacency entry outside [0, n) */
 #define GBX_ERR_TIMEOUT   2u   /* an idle wait exceeded its time limit */
 
@@ -98,6 +105,10 @@ int  gbx_l2_read_probe(size_t bytes, int reps, double *gbs);
 int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots,
                        gbx_ctrl *d_ctrl, gbx_graph_acc *d_acc, int *d_job_levels,
                        unsigned long long spin_limit_ns, int blocks, int active, void *stream);
+
+/* Applies `count` writes, in stream order. */
+int  gbx_scatter(const gbx_write *d_writes, int count, void *stream);
+int  gbx_event_query(void *ev);        /* 0: complete, 1: not yet, else an error */
 
 /* CUDA graphs: capture everything issued on `stream` between begin and end. */
 int  gbx_capture_begin(void *stream);

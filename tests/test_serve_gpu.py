@@ -1,0 +1,112 @@
+"""Serving mode (ODPX_Serve_*): device-resident graphs updated in place by
+2-opt deltas, evaluated in continuous batches.  Every result must equal the
+same graph evaluated alone (a fresh plan) and the oracle, whatever else was
+in flight with it."""
+import threading
+
+import numpy as np
+import pytest
+
+import odp_gb300 as og
+import oracle
+from conftest import same
+
+pytestmark = pytest.mark.gpu
+
+
+def alone(spec_adj, nodes, symmetries):
+    b = og.Batch([og.GraphSpec(spec_adj, nodes=nodes, symmetries=symmetries)])
+    try:
+        return b.run()[0]
+    finally:
+        b.close()
+
+
+def chain_graphs():
+    out = []
+    for i, (n, d, s) in enumerate([(256, 6, 1), (1024, 8, 1), (2048, 12, 4), (4096, 16, 1), (600, 5, 2),
+                                   (3000, 10, 1)]):
+        adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, s, seed=300 + i), d, s)
+        out.append((n, d, s, adj))
+    return out
+
+
+def test_results_alone_and_in_the_mix():
+    srv = og.Server(lanes=3, max_batch=4, max_nodes=4096, memory_mb=256)
+    chains = chain_graphs()
+    handles = [srv.register(og.GraphSpec(adj.copy(), nodes=n, symmetries=s)) for n, d, s, adj in chains]
+    results = {}
+    errors = []
+
+    def run_chain(k):
+        try:
+            n, d, s, adj = chains[k]
+            host = adj.copy()
+            rng = og.Rng(500 + k)
+            for step in range(12):
+                r = rng.mutate_general(n, d, host, symmetries=s)
+                deltas = og.two_opt_deltas(host, r, n, s)
+                rid = srv.submit(handles[k], deltas)
+                got = srv.wait(rid)
+                results[(k, step)] = (got[:3], host.copy())
+        except Exception as e:       # surfaced below
+            errors.append(e)
+
+    threads = [threading.Thread(target=run_chain, args=(k,)) for k in range(len(chains))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    st = srv.stats()
+    assert st["requests_done"] == len(chains) * 12
+    for (k, step), (got, host) in results.items():
+        n, d, s, _ = chains[k]
+        assert same(got, alone(host, n, s)), (k, step)
+        if step % 4 == 0:
+            assert same(got, oracle.aspl(host, nodes=n, symmetries=s)), (k, step)
+    # the resident adjacency followed every delta
+    for k, h in enumerate(handles):
+        assert np.array_equal(srv.adjacency(h), results[(k, 11)][1])
+    srv.close()
+
+
+def test_reject_restores_through_deltas():
+    """An annealing step that is rejected sends the undo of its swap with the
+    next request; the served graph must track the client's copy exactly."""
+    n, d = 1024, 8
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=1), d)
+    srv = og.Server(lanes=2, max_batch=2, max_nodes=2048, memory_mb=64)
+    h = srv.register(og.GraphSpec(adj.copy(), nodes=n))
+    host = adj.copy()
+    rng = og.Rng(7)
+    pending_undo = []
+    current = srv.wait(srv.submit(h))[:3]
+    for step in range(20):
+        r = rng.mutate_general(n, d, host)
+        deltas = pending_undo + og.two_opt_deltas(host, r, n)
+        got = srv.wait(srv.submit(h, deltas))[:3]
+        assert same(got, oracle.aspl(host, nodes=n))
+        if got[2] <= current[2]:
+            current, pending_undo = got, []
+        else:
+            og.restore_adjacency_general(r, host)          # host undo; the server gets it with the next request
+            pending_undo = og.two_opt_deltas(host, r, n)
+    srv.wait(srv.submit(h, pending_undo))
+    assert np.array_equal(srv.adjacency(h), host)
+    srv.close()
+
+
+def test_admission_and_bad_requests():
+    srv = og.Server(lanes=1, max_batch=2, max_nodes=512, memory_mb=16)
+    big = og.conv_edge2adjacency_general(1024, og.generate_random_general(1024, 4, seed=2), 4)
+    with pytest.raises(og.ODPError) as ei:
+        srv.register(og.GraphSpec(big, nodes=1024))
+    assert ei.value.code == og.ERR_MEMORY
+    small = og.conv_edge2adjacency_general(256, og.generate_random_general(256, 4, seed=3), 4)
+    h = srv.register(og.GraphSpec(small, nodes=256))
+    with pytest.raises(og.ODPError) as ei:
+        srv.submit(h, [(0, 0, 999)])
+    assert ei.value.code == og.ERR_ADJACENCY
+    assert same(srv.wait(srv.submit(h))[:3], oracle.aspl(small, nodes=256))
+    srv.close()
