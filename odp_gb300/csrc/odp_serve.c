@@ -28,6 +28,7 @@
 #include <float.h>
 #include <pthread.h>
 #include <time.h>
+#include <sys/prctl.h>
 #include "odp_plan.h"
 #include "odp_gb300.h"
 
@@ -128,7 +129,7 @@ static int lane_init(serve_lane *l, const ODPX_Serve_config *c, int nslots, int 
   l->blocks = blocks;
   l->max_batch = c->max_batch;
   l->max_jobs = c->max_batch * 64;
-  l->max_writes = c->max_batch * 256;
+  l->max_writes = c->max_batch * 4096;
   l->slot_words = ALIGN_UP((size_t)c->max_nodes << c->wc_log2, 32);
   l->slot_rows = ALIGN_UP((size_t)c->max_nodes, 64);
   l->out_off = sizeof(gbx_slot) * (size_t)nslots;
@@ -293,6 +294,9 @@ static int launch_batch(odp_server *s, serve_lane *l)
 static void *scheduler(void *arg)
 {
   odp_server *s = arg;
+  /* the completion polling sleeps for microseconds: keep the kernel from
+   * stretching them by its default 50 us timer slack */
+  prctl(PR_SET_TIMERSLACK, 1UL, 0, 0, 0);
   pthread_mutex_lock(&s->mu);
   while(!s->stop){
     int busy = 0, progress = 0;
@@ -408,6 +412,7 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
     if(g.tile_rows > n) g.tile_rows = n;
   }
   g.ntiles = (n + g.tile_rows - 1) / g.tile_rows;
+  if(g.nchunks > s->lanes[0].max_jobs) return ODPX_ERR_MEMORY;   /* one request must fit a batch */
   size_t adj_ints = (size_t)g.B * g.d;
   g.h_adj = malloc(sizeof(int) * adj_ints);
   memcpy(g.h_adj, gr->adjacency, sizeof(int) * adj_ints);
@@ -488,10 +493,13 @@ int ODPX_Serve_submit(ODPX_Server *s, int handle, int ndelta, const ODPX_Delta *
   pthread_mutex_lock(&s->mu);
   if(handle < 0 || handle >= s->ngraphs){ pthread_mutex_unlock(&s->mu); return ODPX_ERR_INVALID; }
   serve_graph *g = &s->graphs[handle];
+  if((long long)ndelta * (1 + g->s) > s->lanes[0].max_writes){   /* one request must fit a batch */
+    pthread_mutex_unlock(&s->mu);
+    return ODPX_ERR_INVALID;
+  }
   for(int k = 0; k < ndelta; k++){
     const ODPX_Delta *dl = &deltas[k];
-    if(dl->row < 0 || dl->row >= g->B || dl->slot < 0 || dl->slot >= g->d || dl->value < 0 || dl->value >= g->n ||
-       ndelta > 64){
+    if(dl->row < 0 || dl->row >= g->B || dl->slot < 0 || dl->slot >= g->d || dl->value < 0 || dl->value >= g->n){
       pthread_mutex_unlock(&s->mu);
       return ODPX_ERR_ADJACENCY;
     }
