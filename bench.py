@@ -233,7 +233,7 @@ def serving(seconds, rate=20000.0):
             if res[2] <= current or draw.random() < math.exp(-delta / 50.0):
                 current, undo = res[2], []
             else:
-                og.restore_adjacency_general(r, host)
+                og.Rng.restore_general(n, d, r, host)
                 undo = og.two_opt_deltas(host, r, n)
         srv.wait(srv.submit(handles[k], undo))
         with lock:

@@ -93,6 +93,8 @@ void   ODPX_Rng_seed(void *rng_state, unsigned int seed);
 int    ODPX_Rng_next(void *rng_state);
 void   ODPX_Mutate_adjacency_general_s_rng(void *rng_state, int nodes, int degree, const int *num_degrees,
                                            int symmetries, ODP_Restore *r, int *adjacency);
+/* ODP_Restore_adjacency_general with the graph's shape given explicitly. */
+void   ODPX_Restore_adjacency_general_s(int nodes, int degree, int symmetries, ODP_Restore r, int *adjacency);
 
 /* ODPX_Set_aspl_noalloc: no counterpart in the reference.  Evaluates one
  * regular general graph (the arguments of ODP_Init_aspl_general[_s] with

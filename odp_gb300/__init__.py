@@ -107,6 +107,7 @@ def load():
         "ODPX_Rng_seed": (None, [P, ctypes.c_uint]),
         "ODPX_Rng_next": (I, [P]),
         "ODPX_Mutate_adjacency_general_s_rng": (None, [P, I, I, P, I, ctypes.POINTER(Restore), P]),
+        "ODPX_Restore_adjacency_general_s": (None, [I, I, I, Restore, P]),
         "ODPX_Version": (ctypes.c_char_p, []),
     }
     for name, (res, args) in sig.items():
@@ -301,6 +302,11 @@ class Rng:
         load().ODPX_Mutate_adjacency_general_s_rng(self._buf, nodes, degree, _iptr(nd), symmetries,
                                                    ctypes.byref(r), _iptr(adjacency))
         return r
+
+    @staticmethod
+    def restore_general(nodes, degree, r, adjacency, symmetries=1):
+        """Undoes a swap of mutate_general (the shape is given explicitly)."""
+        load().ODPX_Restore_adjacency_general_s(nodes, degree, symmetries, r, _iptr(adjacency))
 
 
 # --------------------------------------------------------------------------

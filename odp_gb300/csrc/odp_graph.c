@@ -52,6 +52,7 @@ typedef struct {              /* a (possibly rotation-symmetric) grid graph */
 
 static inline int wrap(int x, int n)            /* NORM, utils.c:171-177 */
 {
+  if(n <= 0) return x;
   while(x < 0 || x >= n) x = (x < 0) ? x + n : x - n;
   return x;
 }
@@ -1001,14 +1002,27 @@ void odpx_restore_grid(int width, int height, int degree, int symmetries, ODP_Re
   }
 }
 
+/* Restore uses the shape of the last Mutate call, as the reference does
+ * (utils.c:500-507, 461-467); without one there is no shape to use. */
 void ODP_Restore_adjacency_general(ODP_Restore r, void *adjacency)
 {
+  if(m_nodes <= 0 || m_symmetries <= 0) ODP_FAIL("ODP_Restore_adjacency_general called before ODP_Mutate_adjacency_general\n");
   odpx_restore_general(m_nodes, m_degree, m_symmetries, r, adjacency);
 }
 
 void ODP_Restore_adjacency_grid(ODP_Restore r, void *adjacency)
 {
+  if(m_width <= 0 || m_height <= 0 || m_symmetries <= 0)
+    ODP_FAIL("ODP_Restore_adjacency_grid called before ODP_Mutate_adjacency_grid\n");
   odpx_restore_grid(m_width, m_height, m_degree, m_symmetries, r, adjacency);
+}
+
+/* Restore with an explicit shape, for callers that mutate through their own
+ * random streams (ODPX_Mutate_adjacency_general_s_rng). */
+void ODPX_Restore_adjacency_general_s(int nodes, int degree, int symmetries, ODP_Restore r, int *adjacency)
+{
+  if(nodes <= 0 || symmetries <= 0 || nodes % symmetries) ODP_FAIL("nodes(%d) must be divisible by symmetries(%d)\n", nodes, symmetries);
+  odpx_restore_general(nodes, degree, symmetries, r, adjacency);
 }
 
 /* Thread-safe, explicitly parameterised mutate for callers that keep one

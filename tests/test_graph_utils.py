@@ -96,3 +96,28 @@ def test_edge_adjacency_round_trip(s):
     adj = og.conv_edge2adjacency_general(n, e, d, s)
     e2 = og.conv_adjacency2edge_general(n, d, adj, s)
     assert np.array_equal(og.conv_edge2adjacency_general(n, e2, d, s), adj)
+
+
+@pytest.mark.parametrize("s", [1, 2, 8])
+def test_private_stream_mutate_and_explicit_restore(s):
+    n, d = 240, 6
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, s, seed=13), d, s)
+    rng = og.Rng(17)
+    for _ in range(100):
+        before = adj.copy()
+        r = rng.mutate_general(n, d, adj, symmetries=s)
+        og.Rng.restore_general(n, d, r, adj, symmetries=s)
+        assert np.array_equal(before, adj)
+        rng.mutate_general(n, d, adj, symmetries=s)
+
+
+def test_restore_before_any_mutate_is_refused():
+    import subprocess, sys, textwrap
+    from conftest import ROOT
+    code = textwrap.dedent("""
+        import sys; sys.path.insert(0, %r)
+        import numpy as np, odp_gb300 as og
+        og.restore_adjacency_general(og.Restore(), np.zeros((4, 2), dtype=np.int32))
+    """ % ROOT)
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 1 and "before ODP_Mutate" in r.stderr

@@ -90,7 +90,7 @@ def test_reject_restores_through_deltas():
         if got[2] <= current[2]:
             current, pending_undo = got, []
         else:
-            og.restore_adjacency_general(r, host)          # host undo; the server gets it with the next request
+            og.Rng.restore_general(n, d, r, host)          # host undo; the server gets it with the next request
             pending_undo = og.two_opt_deltas(host, r, n)
     srv.wait(srv.submit(h, pending_undo))
     assert np.array_equal(srv.adjacency(h), host)
