@@ -69,7 +69,8 @@ int  ODPX_Batch_job_levels(const ODPX_Batch *batch, int *levels, int max_jobs);
  * stops with ODPX_ERR_TIMEOUT instead of waiting on. */
 void ODPX_Batch_set_wait_limit(ODPX_Batch *batch, unsigned long long ns);
 /* Algorithmic bytes of the last run (roofline numerator): sum over jobs of
- * levels x 8 x words per row x sum over the graph's vertices of (degree + 2). */
+ * levels x 8 x the chunk's source words x sum over the graph's vertices of
+ * (degree + 2). */
 double ODPX_Batch_bytes_alg(const ODPX_Batch *batch);
 /* Read bandwidth (GB/s) of 16-byte L2-only loads streaming an L2-resident
  * buffer of `megabytes`, `reps` times: the L2 ceiling of the roofline. */

@@ -528,7 +528,10 @@ double odp_plan_bytes_alg(const odp_plan *p)
   for(int k = 0; k < p->njobs; k++){
     const gbx_job *j = &p->h_jobs[k];
     int l = lv[k] < 0 ? -lv[k] : lv[k];
-    total += (double)l * 8.0 * (double)(1 << j->wc_log2) * p->g[j->graph].row_reads;
+    /* only the chunk's words that hold sources count; padding words of a
+     * narrow last chunk are moved but are not algorithmic */
+    double words = (double)((j->nsrc + 63) / 64);
+    total += (double)l * 8.0 * words * p->g[j->graph].row_reads;
   }
   return total;
 }

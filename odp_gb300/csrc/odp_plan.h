@@ -90,8 +90,8 @@ unsigned int odp_plan_error(const odp_plan *p);
 /* Level at which each job (in plan order) finished; negative if it stalled. */
 const int *odp_plan_job_levels(const odp_plan *p);
 int odp_plan_enqueue_engine(odp_plan *p);
-/* Algorithmic bytes of the last run: sum over jobs of
- * |level| x 8 x words-per-row x row_reads of the job's graph. */
+/* Algorithmic bytes of the last run: sum over jobs of |level| x 8 x the
+ * chunk's source words (ceil(nsrc / 64)) x row_reads of the job's graph. */
 double odp_plan_bytes_alg(const odp_plan *p);
 
 /* Device bring-up shared by every entry point; exits through ODP_FAIL-like
