@@ -339,10 +339,20 @@ class GraphSpec:
         return g
 
 
+_batch_arrays = {}
+
+
 def set_aspl_batch(specs):
     """ODP_Set_aspl_batch: list of (diameter, sum, ASPL), one per spec."""
     n = len(specs)
-    arr = (Graph * n)(*[s.to_c() for s in specs])
+    # the ODP_Graph array is rebuilt only when a spec or one of its arrays changes
+    key = tuple((id(s), s.adjacency.ctypes.data, 0 if s.num_degrees is None else s.num_degrees.ctypes.data)
+                for s in specs)
+    arr = _batch_arrays.get(key)
+    if arr is None:
+        arr = (Graph * n)(*[s.to_c() for s in specs])
+        _batch_arrays.clear()
+        _batch_arrays[key] = arr
     d = np.zeros(n, dtype=np.int32)
     s = np.zeros(n, dtype=np.int64)
     a = np.zeros(n, dtype=np.float64)

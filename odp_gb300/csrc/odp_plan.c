@@ -18,6 +18,8 @@
 #include <string.h>
 #include <limits.h>
 #include <float.h>
+#include <pthread.h>
+#include <unistd.h>
 #include "odp_plan.h"
 #include "odp_gb300.h"
 
@@ -452,11 +454,55 @@ const int *odp_plan_job_levels(const odp_plan *p)
   return (const int *)(p->h_state_out + (p->levels_off - p->out_off));
 }
 
+typedef struct {
+  odp_plan *p;
+  const int *const *adjacency;
+  int first, last;
+} stage_part;
+
+static void *stage_worker(void *arg)
+{
+  stage_part *w = arg;
+  for(int i = w->first; i < w->last; i++){
+    const odp_plan_graph *g = &w->p->g[i];
+    memcpy(w->p->h_adj + g->adj_off, w->adjacency[i], sizeof(int) * g->adj_ints);
+  }
+  return NULL;
+}
+
+/* Copies the callers' adjacency arrays into the pinned staging buffer that
+ * the upload reads.  Large batches are split over host threads by bytes:
+ * one thread copies at a fraction of the memory bandwidth. */
 void odp_plan_stage(odp_plan *p, const int *const *adjacency)
 {
-  for(int i = 0; i < p->ngraphs; i++){
-    const odp_plan_graph *g = &p->g[i];
-    memcpy(p->h_adj + g->adj_off, adjacency[i], sizeof(int) * g->adj_ints);
+  size_t total = sizeof(int) * p->adj_ints;
+  long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+  int nt = total < (4u << 20) ? 1 : (int)(cpus < 16 ? cpus : 16);
+  if(nt > p->ngraphs) nt = p->ngraphs;
+  if(nt <= 1){
+    stage_part w = { p, adjacency, 0, p->ngraphs };
+    stage_worker(&w);
+    return;
+  }
+  stage_part parts[16];
+  pthread_t th[16];
+  size_t per = total / (size_t)nt, acc = 0;
+  int start = 0, k = 0;
+  for(int i = 0; i < p->ngraphs && k < nt - 1; i++){
+    acc += sizeof(int) * p->g[i].adj_ints;
+    if(acc >= per * (size_t)(k + 1)){
+      parts[k] = (stage_part){ p, adjacency, start, i + 1 };
+      start = i + 1;
+      k++;
+    }
+  }
+  parts[k++] = (stage_part){ p, adjacency, start, p->ngraphs };
+  int launched[16] = {0};
+  for(int t = 1; t < k; t++) launched[t] = pthread_create(&th[t], NULL, stage_worker, &parts[t]) == 0;
+  stage_worker(&parts[0]);
+  for(int t = 1; t < k; t++){
+    if(launched[t]) pthread_join(th[t], NULL);
+    else stage_worker(&parts[t]);
   }
 }
 
