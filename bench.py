@@ -64,6 +64,7 @@ def parse():
     p.add_argument("--no-per-call", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-tune", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=8.0)
     return p.parse_args()
 
@@ -291,6 +292,10 @@ def run_own(args):
     count = len(specs)
     adj_bytes = int(sum(s.adjacency.nbytes for s in specs))
 
+    # ---- autotune the schedule for this batch (outside every timed region) ----
+    from odp_gb300 import autotune
+    tune_report = autotune.tune_batch(specs) if not args.no_tune else None
+
     # ---- batched engine on resident inputs (headline) ----
     batch = og.Batch(specs)
     res = batch.run()
@@ -326,7 +331,10 @@ def run_own(args):
             "e2e": {"value": world * count / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": adj_bytes,
                     "d2h_bytes_per_step": 16 * count + 128},
             "gpu_launches": args.steps,
-            "batch_device_ms_with_transfers": ms_full}
+            "batch_device_ms_with_transfers": ms_full,
+            "autotune": tune_report}
+
+    autotune.clear()
 
     # ---- one graph per call on the same GPU ----
     if not args.no_per_call:
@@ -364,6 +372,7 @@ def run_own(args):
     # ---- the single large graph (MATRIX_SAVING configuration) ----
     if not args.no_single:
         adj = single_graph()
+        single_tune = autotune.tune_single(og.GraphSpec(adj, nodes=C2["nodes"])) if not args.no_tune else None
         sb = og.Batch([og.GraphSpec(adj, nodes=C2["nodes"])])
         r = sb.run()[0]
         assert r[:2] == C2["result"], r
@@ -382,8 +391,9 @@ def run_own(args):
         line["single_graph"] = {"workload": "n=65536 d=16 seed=2 (MATRIX_SAVING config)", "evals_per_s": 1000.0 / sms,
                                 "ms": sms, "e2e_evals_per_s": 1.0 / s_e2e, "bytes_alg": sbytes,
                                 "achieved_gbs": sbytes / (sms * 1e-3) / 1e9, "chunk_words": 1 << sinfo["wc_log2"],
-                                "slots": sinfo["nslots"], "tile_rows": sinfo["tile_rows"],
+                                "slots": sinfo["nslots"], "tile_rows": sinfo["tile_rows"], "autotune": single_tune,
                                 "result": {"diameter": r[0], "sum": r[1], "ASPL": r[2]}}
+        autotune.clear()
 
     if not args.no_serving and world == 1:
         line["serving"] = serving(args.serve_seconds)

@@ -80,6 +80,19 @@ double ODPX_Measure_l2_read_gbs(int megabytes, int reps);
  * -1 automatic, 0 off, 1 on). */
 void ODPX_Set_tuning(int wc_log2, int slots, int tile_rows, int l2_budget_mb, int local_kb, int use_graph);
 
+/* Per-bucket tuning table consulted when plans are created (the autotuner
+ * in odp_gb300/autotune.py fills it).  A graph matches an entry by
+ * ceil(log2 n), degree class (ODPX_Degree_class) and grid flag; fields <= 0
+ * keep the built-in choice.  ODPX_Set_tuning overrides take precedence. */
+typedef struct {
+  int n_log2, degree_class, grid;
+  int wc_log2;               /* chunk width: 2^wc_log2 words, i.e. 2^wc_log2 / 2 lanes per row (<= 32) */
+  int tile_kb;               /* traffic per row tile */
+  int local_kb;              /* per-level traffic at or below which one CTA runs the whole job */
+} ODPX_Tune_entry;
+int ODPX_Set_tuning_table(const ODPX_Tune_entry *entries, int count);
+int ODPX_Degree_class(int degree);
+
 /* Drop-in introspection: the plan behind the current ODP_Init_aspl_* state. */
 ODPX_Batch *ODPX_Current_plan(void);
 

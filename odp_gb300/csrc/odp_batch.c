@@ -33,7 +33,7 @@ static void tuning_for(int count, odp_tuning *t)
   if(g_override.slots > 0) t->slots = g_override.slots;
   if(g_override.tile_rows > 0) t->tile_rows = g_override.tile_rows;
   if(g_override.l2_budget_mb > 0) t->l2_budget_mb = g_override.l2_budget_mb;
-  if(g_override.local_kb > 0) t->local_kb = g_override.local_kb;
+  if(g_override.local_kb > 0){ t->local_kb = g_override.local_kb; t->local_kb_explicit = 1; }
   if(g_override.use_graph >= 0) t->use_graph = g_override.use_graph;
 }
 

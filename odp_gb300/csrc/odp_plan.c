@@ -52,6 +52,7 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->use_graph = env_int("ODP_GB300_GRAPH", 1);
   t->blocks = env_int("ODP_GB300_BLOCKS", 0);
   t->activity = env_int("ODP_GB300_ACTIVITY", 0);
+  t->local_kb_explicit = getenv("ODP_GB300_LOCAL_KB") != NULL;
 }
 
 static int ilog2_ceil(long long x)
@@ -171,6 +172,32 @@ static void fill_srcpos(const odp_plan_graph *g, int *srcpos)
         }
 }
 
+/* Per-bucket tuning table (ODPX_Set_tuning_table), filled by the autotuner:
+ * a graph whose (ceil log2 n, degree class, grid) matches an entry takes its
+ * chunk width, tile traffic and local-job threshold. */
+#define TUNE_MAX 256
+static ODPX_Tune_entry g_table[TUNE_MAX];
+static int g_table_len = 0;
+
+int ODPX_Set_tuning_table(const ODPX_Tune_entry *entries, int count)
+{
+  if(count < 0 || count > TUNE_MAX || (count > 0 && !entries)) return ODPX_ERR_INVALID;
+  if(count) memcpy(g_table, entries, sizeof(ODPX_Tune_entry) * (size_t)count);
+  g_table_len = count;
+  return 0;
+}
+
+int ODPX_Degree_class(int degree) { return degree <= 8 ? 0 : degree <= 16 ? 1 : degree <= 32 ? 2 : 3; }
+
+static const ODPX_Tune_entry *table_lookup(int n, int degree, int grid)
+{
+  int nl = ilog2_ceil(n);
+  int dc = ODPX_Degree_class(degree);
+  for(int i = 0; i < g_table_len; i++)
+    if(g_table[i].n_log2 == nl && g_table[i].degree_class == dc && g_table[i].grid == grid) return &g_table[i];
+  return NULL;
+}
+
 typedef struct { int job; double work; } job_order;
 
 static int cmp_work_desc(const void *a, const void *b)
@@ -219,8 +246,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     g->B = g->n / g->s;
     g->W = (g->B + 63) / 64;
     int full_l2 = ilog2_ceil(g->W < 2 ? 2 : g->W);
+    const ODPX_Tune_entry *te = table_lookup(g->n, g->d, g->grid);
     int wl;
     if(tuning->wc_log2 > 0) wl = tuning->wc_log2;
+    else if(te && te->wc_log2 > 0) wl = te->wc_log2;
     else if(count > 1){
       /* batch: 256-byte rows, 64 concurrent jobs (measured best on GB300 for
        * the 512-graph workload) */
@@ -240,11 +269,14 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     g->nchunks = (g->W + wc - 1) / wc;
     double level_bytes = (double)g->n * wc * 8.0 * (g->d + 2);
     int rpp = rows_per_pass(wl);
+    double local_here = (te && te->local_kb > 0 && tuning->local_kb_explicit == 0) ? te->local_kb * 1024.0
+                                                                                   : local_bytes;
+    double tile_bytes = (te && te->tile_kb > 0) ? te->tile_kb * 1024.0 : 288.0 * 1024.0;
     if(tuning->tile_rows > 0) g->tile_rows = tuning->tile_rows;
-    else if(level_bytes <= local_bytes) g->tile_rows = g->n;
+    else if(level_bytes <= local_here) g->tile_rows = g->n;
     else{
       double per_row = (double)wc * 8.0 * (g->d + 2);
-      int tr = (int)(288.0 * 1024.0 / per_row);
+      int tr = (int)(tile_bytes / per_row);
       g->tile_rows = ALIGN_UP(tr < rpp ? rpp : tr, rpp);
     }
     if(g->tile_rows > g->n) g->tile_rows = g->n;

@@ -29,6 +29,7 @@ typedef struct {
   int use_graph;               /* replay through a CUDA graph */
   int blocks;                  /* persistent grid size; 0 = SMs x occupancy */
   int activity;                /* change tracking: 0 never (default), 1 always, -1 grids only */
+  int local_kb_explicit;       /* local_kb was set by the caller: the tuning table does not override it */
 } odp_tuning;
 
 typedef struct {
