@@ -349,6 +349,7 @@ def main():
                  "oracle/Makefile) through tests/golden/make_golden.py; results are [diameter, sum, "
                  "ASPL as float.hex].",
         "samples": samples(),
+        "sample_text": {k: open(os.path.join(REF, "sample/graph/%s/ASPL.txt" % k)).read() for k in ("general", "grid")},
         "generators": generators(big),
         "cases": cases(),
         "mutations": mutations(),

@@ -1,0 +1,62 @@
+"""The multi-process (torchrun) paths of bench.py on CPU with 2 gloo ranks:
+every rank runs its own replica, rank 0 alone prints one JSON line, and the
+timing is the maximum over ranks."""
+import json
+import os
+import socket
+import subprocess
+import sys
+
+import pytest
+
+from conftest import ROOT
+
+
+def free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def test_reference_arm_under_torchrun_prints_once():
+    pytest.importorskip("torch")
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.join(ROOT, "bench.py"),
+           "--impl", "reference", "--gpus", "2", "--graphs", "12", "--steps", "1", "--warmup", "1",
+           "--cpu-seconds", "0.5"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=280, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    rec = json.loads(lines[0])
+    assert rec["impl"] == "reference" and rec["n_gpus"] == 2 and rec["value"] > 0
+
+
+WORKER = r"""
+import os, sys, json
+sys.path.insert(0, %r)
+import bench
+rank, world, _ = bench.dist_info()
+d = bench.Dist(world)
+d.barrier()
+local_ms = 10.0 + 5.0 * rank
+m = d.max(local_ms)
+d.barrier()
+if rank == 0:
+    print(json.dumps({"max_ms": m, "value": world * 100 * 1000.0 / m}))
+"""
+
+
+def test_dist_helper_takes_the_max_over_ranks(tmp_path):
+    pytest.importorskip("torch")
+    script = tmp_path / "worker.py"
+    script.write_text(WORKER % ROOT)
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+           "--master-addr", "127.0.0.1", "--master-port", str(free_port()), str(script)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=200)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rec = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][0])
+    assert rec["max_ms"] == 15.0
+    assert abs(rec["value"] - 2 * 100 * 1000.0 / 15.0) < 1e-9
