@@ -65,6 +65,10 @@ int  ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots
 /* Level at which each job (graph x column chunk, plan order) of the last run
  * finished (negative: stalled, i.e. unreachable pairs).  Returns the job count. */
 int  ODPX_Batch_job_levels(const ODPX_Batch *batch, int *levels, int max_jobs);
+/* Per job of the last run (plan order): its graph and the device times (us,
+ * from the earliest stamp) at which it was loaded into a slot (0: before the
+ * launch) and finished.  Returns the job count. */
+int  ODPX_Batch_job_profile(const ODPX_Batch *batch, int *graph, double *loaded_us, double *done_us, int max_jobs);
 /* Time limit of the engine's idle waits (default 60 s); past it the run
  * stops with ODPX_ERR_TIMEOUT instead of waiting on. */
 void ODPX_Batch_set_wait_limit(ODPX_Batch *batch, unsigned long long ns);

@@ -98,6 +98,7 @@ def load():
         "ODPX_Batch_tiles": (ctypes.c_ulonglong, [P]),
         "ODPX_Batch_info": (I, [P, I, IP, IP, IP, IP]),
         "ODPX_Batch_job_levels": (I, [P, IP, I]),
+        "ODPX_Batch_job_profile": (I, [P, IP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), I]),
         "ODPX_Batch_set_wait_limit": (None, [P, ctypes.c_ulonglong]),
         "ODPX_Batch_bytes_alg": (ctypes.c_double, [P]),
         "ODPX_Measure_l2_read_gbs": (ctypes.c_double, [I, I]),
@@ -418,6 +419,17 @@ class Batch:
     def bytes_alg(self):
         """Algorithmic bytes of the last run (roofline numerator)."""
         return float(load().ODPX_Batch_bytes_alg(self._h))
+
+    def job_profile(self):
+        """(graph, loaded_us, done_us) arrays per job of the last run (plan order)."""
+        n = self.info(0)["njobs"]
+        g = np.zeros(n, dtype=np.int32)
+        a = np.zeros(n, dtype=np.float64)
+        b = np.zeros(n, dtype=np.float64)
+        load().ODPX_Batch_job_profile(self._h, g.ctypes.data_as(ctypes.POINTER(ctypes.c_int)),
+                                      a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)),
+                                      b.ctypes.data_as(ctypes.POINTER(ctypes.c_double)), n)
+        return g, a, b
 
     def set_wait_limit(self, ns):
         load().ODPX_Batch_set_wait_limit(self._h, int(ns))

@@ -447,7 +447,7 @@ __device__ __forceinline__ bool take_tile(gbx_slot *slots, int nslots, int &curs
 
 __global__ void __launch_bounds__(ENGINE_THREADS, ENGINE_MIN_BLOCKS)
 engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int nslots, gbx_ctrl *ctrl,
-              gbx_graph_acc *acc, int *job_levels, unsigned long long spin_limit_ns)
+              gbx_graph_acc *acc, gbx_job_out *job_out, unsigned long long spin_limit_ns)
 {
   __shared__ gbx_job sh_job;
   __shared__ int sh_state, sh_slot, sh_tile, sh_level;
@@ -559,13 +559,15 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
           }
           else{
             gbx_graph_acc *ga = &acc[jb.graph];
-            job_levels[sl->job] = stalled ? -level : level;
+            job_out[sl->job].level = stalled ? -level : level;
+            job_out[sl->job].t_done = globaltimer();
             atomicAdd(&ga->sum, (unsigned long long)sl->sum);
             atomicMax(&ga->levels, level);
             if(stalled) atomicOr(&ga->flags, 1);
             unsigned j = atomicAdd(&ctrl->next_job, 1u);
             if(j < (unsigned)njobs){
               const gbx_job nj = jobs[j];
+              job_out[j].t_loaded = globaltimer();
               sl->job = (int)j;
               sl->level = 1;
               sl->count = 0;
@@ -730,14 +732,14 @@ int gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertic
 }
 
 int gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots, gbx_ctrl *d_ctrl,
-                      gbx_graph_acc *d_acc, int *d_job_levels, unsigned long long spin_limit_ns, int blocks,
+                      gbx_graph_acc *d_acc, gbx_job_out *d_job_out, unsigned long long spin_limit_ns, int blocks,
                       int active, void *stream)
 {
   if(njobs <= 0 || nslots <= 0) return 0;
   if(blocks <= 0) blocks = gbx_engine_blocks(active);
   if(blocks <= 0) blocks = 1;
   engine_kernel<<<blocks, ENGINE_THREADS, active ? STAGE_BYTES_ACTIVE : STAGE_BYTES_PLAIN,
-                  (cudaStream_t)stream>>>(d_jobs, njobs, d_slots, nslots, d_ctrl, d_acc, d_job_levels,
+                  (cudaStream_t)stream>>>(d_jobs, njobs, d_slots, nslots, d_ctrl, d_acc, d_job_out,
                                           spin_limit_ns);
   return (int)cudaGetLastError();
 }
@@ -898,7 +900,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
     out_off = sizeof(gbx_slot) * (size_t)nslots;
     acc_off = out_off + sizeof(gbx_ctrl) + 64;
     levels_off = acc_off + 64;
-    state_bytes = levels_off + sizeof(int) * (size_t)njobs;
+    state_bytes = levels_off + sizeof(gbx_job_out) * (size_t)njobs;
     off_buf = up256(off_state + state_bytes);
     off_mask = up256(off_buf + sizeof(unsigned long long) * 2 * (size_t)nslots * ((size_t)n << wl));
     total = off_mask + sizeof(unsigned) * 2 * (size_t)nslots * (size_t)n;
@@ -949,7 +951,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   /* The array keeps whatever the previous call left in it: the engine state
    * is rewritten here in full; the neighbour table and the bitset buffers
    * are overwritten by the kernels before they are read. */
-  unsigned char state[sizeof(gbx_slot) * 2 + sizeof(gbx_ctrl) + 64 + 64 + sizeof(int) * NOALLOC_MAX_JOBS];
+  unsigned char state[sizeof(gbx_slot) * 2 + sizeof(gbx_ctrl) + 64 + 64 + sizeof(gbx_job_out) * NOALLOC_MAX_JOBS];
   memset(state, 0, sizeof(state));
   gbx_slot *sl = (gbx_slot *)state;
   unsigned long long *bufs = (unsigned long long *)(base + off_buf);
@@ -978,7 +980,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   engine_kernel<<<nd->blocks, ENGINE_THREADS, STAGE_BYTES_PLAIN, st>>>(
       (const gbx_job *)(base + off_jobs), njobs, (gbx_slot *)(base + off_state), nslots,
       (gbx_ctrl *)(base + off_state + out_off), (gbx_graph_acc *)(base + off_state + acc_off),
-      (int *)(base + off_state + levels_off), 60ull * 1000000000ull);
+      (gbx_job_out *)(base + off_state + levels_off), 60ull * 1000000000ull);
   if(cudaGetLastError() != cudaSuccess) return ODPX_ERR_CUDA;
   unsigned char out[sizeof(gbx_ctrl) + 64 + 64];
   if(cudaMemcpyAsync(out, base + off_state + out_off, sizeof(out), cudaMemcpyDeviceToHost, st) ||

@@ -223,9 +223,27 @@ int ODPX_Batch_time(ODPX_Batch *batch, const int *const *adjacency, int repeats,
 int ODPX_Batch_job_levels(const ODPX_Batch *batch, int *levels, int max_jobs)
 {
   if(!batch) return ODPX_ERR_STATE;
-  const int *l = odp_plan_job_levels(batch);
+  const gbx_job_out *jo = odp_plan_job_out(batch);
   int n = batch->njobs < max_jobs ? batch->njobs : max_jobs;
-  for(int i = 0; i < n; i++) levels[i] = l[i];
+  for(int i = 0; i < n; i++) levels[i] = jo[i].level;
+  return batch->njobs;
+}
+
+int ODPX_Batch_job_profile(const ODPX_Batch *batch, int *graph, double *loaded_us, double *done_us, int max_jobs)
+{
+  if(!batch) return ODPX_ERR_STATE;
+  const gbx_job_out *jo = odp_plan_job_out(batch);
+  int n = batch->njobs < max_jobs ? batch->njobs : max_jobs;
+  unsigned long long t0 = ~0ull;
+  for(int i = 0; i < batch->njobs; i++){
+    if(jo[i].t_loaded && jo[i].t_loaded < t0) t0 = jo[i].t_loaded;
+    if(jo[i].t_done && jo[i].t_done < t0) t0 = jo[i].t_done;
+  }
+  for(int i = 0; i < n; i++){
+    if(graph) graph[i] = batch->h_jobs[i].graph;
+    loaded_us[i] = jo[i].t_loaded ? (double)(jo[i].t_loaded - t0) * 1e-3 : 0.0;
+    done_us[i] = (double)(jo[i].t_done - t0) * 1e-3;
+  }
   return batch->njobs;
 }
 

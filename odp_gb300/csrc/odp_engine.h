@@ -72,6 +72,15 @@ typedef struct {
   int flags;                   /* 1: some chunk stalled (disconnected) */
 } gbx_graph_acc;
 
+/* Per-job outcome: the level at which the job finished (negative: it
+ * stalled) and %globaltimer stamps of when it was loaded into a slot (0 for
+ * jobs loaded by the host before the launch) and when it finished. */
+typedef struct {
+  int level;
+  int pad;
+  unsigned long long t_loaded, t_done;
+} gbx_job_out;
+
 /* One int write into device memory (served-graph updates). */
 typedef struct {
   int *at;
@@ -103,7 +112,7 @@ int  gbx_engine_blocks(int active);    /* persistent grid size (SMs x resident C
 /* Streaming read bandwidth of an L2-resident buffer of `bytes` (GB/s). */
 int  gbx_l2_read_probe(size_t bytes, int reps, double *gbs);
 int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots,
-                       gbx_ctrl *d_ctrl, gbx_graph_acc *d_acc, int *d_job_levels,
+                       gbx_ctrl *d_ctrl, gbx_graph_acc *d_acc, gbx_job_out *d_job_out,
                        unsigned long long spin_limit_ns, int blocks, int active, void *stream);
 
 /* Applies `count` writes, in stream order. */

@@ -362,7 +362,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   p->out_off = sizeof(gbx_slot) * (size_t)nslots;
   p->acc_off = p->out_off + sizeof(gbx_ctrl) + 64;
   p->levels_off = p->acc_off + ALIGN_UP(sizeof(gbx_graph_acc) * (size_t)count, 64);
-  p->state_bytes = p->levels_off + ALIGN_UP(sizeof(int) * (size_t)njobs, 64);
+  p->state_bytes = p->levels_off + ALIGN_UP(sizeof(gbx_job_out) * (size_t)njobs, 64);
   p->out_bytes = p->state_bytes - p->out_off;
 
   CK(gbx_stream_create(&p->stream));
@@ -477,13 +477,13 @@ int odp_plan_enqueue_engine(odp_plan *p)
 {
   return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
                            (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),
-                           (int *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->any_active,
+                           (gbx_job_out *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->any_active,
                            p->stream);
 }
 
-const int *odp_plan_job_levels(const odp_plan *p)
+const gbx_job_out *odp_plan_job_out(const odp_plan *p)
 {
-  return (const int *)(p->h_state_out + (p->levels_off - p->out_off));
+  return (const gbx_job_out *)(p->h_state_out + (p->levels_off - p->out_off));
 }
 
 typedef struct {
@@ -601,11 +601,11 @@ unsigned int odp_plan_error(const odp_plan *p)
 
 double odp_plan_bytes_alg(const odp_plan *p)
 {
-  const int *lv = odp_plan_job_levels(p);
+  const gbx_job_out *jo = odp_plan_job_out(p);
   double total = 0;
   for(int k = 0; k < p->njobs; k++){
     const gbx_job *j = &p->h_jobs[k];
-    int l = lv[k] < 0 ? -lv[k] : lv[k];
+    int l = jo[k].level < 0 ? -jo[k].level : jo[k].level;
     /* only the chunk's words that hold sources count; padding words of a
      * narrow last chunk are moved but are not algorithmic */
     double words = (double)((j->nsrc + 63) / 64);

@@ -88,8 +88,9 @@ int  odp_plan_finish(odp_plan *p, odp_result *results);
 /* Last run's device counters. */
 unsigned long long odp_plan_tiles(const odp_plan *p);
 unsigned int odp_plan_error(const odp_plan *p);
-/* Level at which each job (in plan order) finished; negative if it stalled. */
-const int *odp_plan_job_levels(const odp_plan *p);
+/* Outcome of each job (plan order): level (negative if it stalled) and
+ * device timestamps of its load and finish. */
+const gbx_job_out *odp_plan_job_out(const odp_plan *p);
 int odp_plan_enqueue_engine(odp_plan *p);
 /* Algorithmic bytes of the last run: sum over jobs of |level| x 8 x the
  * chunk's source words (ceil(nsrc / 64)) x row_reads of the job's graph. */

@@ -135,7 +135,7 @@ static int lane_init(serve_lane *l, const ODPX_Serve_config *c, int nslots, int 
   l->out_off = sizeof(gbx_slot) * (size_t)nslots;
   l->acc_off = l->out_off + sizeof(gbx_ctrl) + 64;
   l->levels_off = l->acc_off + ALIGN_UP(sizeof(gbx_graph_acc) * (size_t)l->max_batch, 64);
-  l->state_bytes = l->levels_off + ALIGN_UP(sizeof(int) * (size_t)l->max_jobs, 64);
+  l->state_bytes = l->levels_off + ALIGN_UP(sizeof(gbx_job_out) * (size_t)l->max_jobs, 64);
   if(gbx_stream_create(&l->stream) || gbx_event_create(&l->ev) ||
      gbx_malloc((void **)&l->d_slotbuf, sizeof(unsigned long long) * l->slot_words * 2 * (size_t)nslots) ||
      gbx_malloc((void **)&l->d_slotmask, sizeof(unsigned) * l->slot_rows * 2 * (size_t)nslots) ||
@@ -262,14 +262,14 @@ static int launch_batch(odp_server *s, serve_lane *l)
   }
   ((gbx_ctrl *)(l->h_state + l->out_off))->next_job = (unsigned)nslots;
   /* slots past nslots stay empty (ticket 0); the engine retires them */
-  size_t out_bytes = l->levels_off + sizeof(int) * (size_t)njobs - l->out_off;
+  size_t out_bytes = l->levels_off + sizeof(gbx_job_out) * (size_t)njobs - l->out_off;
   int e = 0;
   if(nw) e |= gbx_memcpy_h2d(l->d_writes, l->h_writes, sizeof(gbx_write) * (size_t)nw, l->stream);
   if(nw) e |= gbx_scatter(l->d_writes, nw, l->stream);
   e |= gbx_memcpy_h2d(l->d_jobs, l->h_jobs, sizeof(gbx_job) * (size_t)njobs, l->stream);
   e |= gbx_memcpy_h2d(l->d_state, l->h_state, l->levels_off, l->stream);
   e |= gbx_engine_launch(l->d_jobs, njobs, (gbx_slot *)l->d_state, nslots, (gbx_ctrl *)(l->d_state + l->out_off),
-                         (gbx_graph_acc *)(l->d_state + l->acc_off), (int *)(l->d_state + l->levels_off),
+                         (gbx_graph_acc *)(l->d_state + l->acc_off), (gbx_job_out *)(l->d_state + l->levels_off),
                          60ull * 1000000000ull, l->blocks, 0, l->stream);
   e |= gbx_memcpy_d2h(l->h_out, l->d_state + l->out_off, out_bytes, l->stream);
   e |= gbx_event_record(l->ev, l->stream);
