@@ -66,8 +66,10 @@ int  ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots
  * finished (negative: stalled, i.e. unreachable pairs).  Returns the job count. */
 int  ODPX_Batch_job_levels(const ODPX_Batch *batch, int *levels, int max_jobs);
 /* Per job of the last run (plan order): its graph and the device times (us,
- * from the earliest stamp) at which it was loaded into a slot (0: before the
- * launch) and finished.  Returns the job count. */
+ * from the start of the engine kernel) at which it was loaded into a slot
+ * (0: before the launch) and finished.  Returns the job count.  After the
+ * first run of a plan the jobs are ordered by their measured durations,
+ * longest first (ODP_GB300_REORDER=0 keeps the first order). */
 int  ODPX_Batch_job_profile(const ODPX_Batch *batch, int *graph, double *loaded_us, double *done_us, int max_jobs);
 /* Time limit of the engine's idle waits (default 60 s); past it the run
  * stops with ODPX_ERR_TIMEOUT instead of waiting on. */

@@ -461,6 +461,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
 
   int cursor = blockIdx.x % nslots;
   unsigned long long idle_since = 0;
+  if(blockIdx.x == 0 && threadIdx.x == 0) ctrl->t_start = globaltimer();
   int pre_slot = -1, pre_tile = 0;      /* thread 0: a ticket taken ahead of time */
 
   for(;;){

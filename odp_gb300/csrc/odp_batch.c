@@ -234,7 +234,7 @@ int ODPX_Batch_job_profile(const ODPX_Batch *batch, int *graph, double *loaded_u
   if(!batch) return ODPX_ERR_STATE;
   const gbx_job_out *jo = odp_plan_job_out(batch);
   int n = batch->njobs < max_jobs ? batch->njobs : max_jobs;
-  unsigned long long t0 = ~0ull;
+  unsigned long long t0 = ((const gbx_ctrl *)batch->h_state_out)->t_start;
   for(int i = 0; i < batch->njobs; i++){
     if(jo[i].t_loaded && jo[i].t_loaded < t0) t0 = jo[i].t_loaded;
     if(jo[i].t_done && jo[i].t_done < t0) t0 = jo[i].t_done;

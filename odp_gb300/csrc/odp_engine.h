@@ -63,7 +63,8 @@ typedef struct {
   unsigned int error;          /* GBX_ERR_* bits */
   unsigned int pad;
   unsigned long long tiles;    /* tiles processed */
-  unsigned long long pad1[5];  /* 64 bytes */
+  unsigned long long t_start;  /* %globaltimer when CTA 0 started */
+  unsigned long long pad1[4];  /* 64 bytes */
 } gbx_ctrl;
 
 typedef struct {

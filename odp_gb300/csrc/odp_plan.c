@@ -53,6 +53,7 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->blocks = env_int("ODP_GB300_BLOCKS", 0);
   t->activity = env_int("ODP_GB300_ACTIVITY", 0);
   t->local_kb_explicit = getenv("ODP_GB300_LOCAL_KB") != NULL;
+  t->reorder = env_int("ODP_GB300_REORDER", 1);
 }
 
 static int ilog2_ceil(long long x)
@@ -206,6 +207,28 @@ static int cmp_work_desc(const void *a, const void *b)
   if(wa > wb) return -1;
   if(wa < wb) return 1;
   return ((const job_order *)a)->job - ((const job_order *)b)->job;
+}
+
+/* Initial engine state: the first nslots jobs loaded into the slots, the
+ * job queue at nslots, everything else zero. */
+static void fill_state_init(odp_plan *p)
+{
+  memset(p->h_state_init, 0, p->state_bytes);
+  gbx_slot *sl = (gbx_slot *)p->h_state_init;
+  for(int k = 0; k < p->nslots; k++){
+    const gbx_job *j = &p->h_jobs[k];
+    sl[k].ticket = (unsigned long long)j->ntiles << 32;
+    sl[k].job = k;
+    sl[k].level = 1;
+    sl[k].prev = (unsigned long long)j->nsrc;
+    sl[k].sum = ((long long)j->n * j->nsrc - j->nsrc) * j->sym;
+    sl[k].buf0 = p->d_slotbuf + (size_t)k * 2 * p->slot_words;
+    sl[k].buf1 = sl[k].buf0 + p->slot_words;
+    sl[k].mask0 = p->d_slotmask + (size_t)k * 2 * p->slot_rows;
+    sl[k].mask1 = sl[k].mask0 + p->slot_rows;
+  }
+  gbx_ctrl *ctrl = (gbx_ctrl *)(p->h_state_init + p->out_off);
+  ctrl->next_job = (unsigned)p->nslots;
 }
 
 #define CK(call) do{ int _e = (call); if(_e){ rc = ODPX_ERR_CUDA; goto fail; } }while(0)
@@ -421,25 +444,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     free(h_nd); free(h_it); free(h_sp); free(ed);
   }
 
-  /* Initial engine state: the first nslots jobs loaded into the slots. */
-  {
-    memset(p->h_state_init, 0, p->state_bytes);
-    gbx_slot *sl = (gbx_slot *)p->h_state_init;
-    for(int k = 0; k < nslots; k++){
-      const gbx_job *j = &p->h_jobs[k];
-      sl[k].ticket = (unsigned long long)j->ntiles << 32;
-      sl[k].job = k;
-      sl[k].level = 1;
-      sl[k].prev = (unsigned long long)j->nsrc;
-      sl[k].sum = ((long long)j->n * j->nsrc - j->nsrc) * j->sym;
-      sl[k].buf0 = p->d_slotbuf + (size_t)k * 2 * p->slot_words;
-      sl[k].buf1 = sl[k].buf0 + p->slot_words;
-      sl[k].mask0 = p->d_slotmask + (size_t)k * 2 * p->slot_rows;
-      sl[k].mask1 = sl[k].mask0 + p->slot_rows;
-    }
-    gbx_ctrl *ctrl = (gbx_ctrl *)(p->h_state_init + p->out_off);
-    ctrl->next_job = (unsigned)nslots;
-  }
+  fill_state_init(p);
   *out = p;
   return 0;
 
@@ -554,6 +559,47 @@ int odp_plan_launch(odp_plan *p)
   return enqueue(p) ? ODPX_ERR_CUDA : 0;
 }
 
+/* Longest-processing-time order learned from a finished run.  The first
+ * order sorts jobs by their per-level traffic, which does not know how many
+ * levels each job will run; a graph with a long diameter (a grid with a short
+ * length limit) then starts late and ends the batch alone.  After the first
+ * run the jobs are re-sorted by their measured device time (load to finish),
+ * so the next runs start the longest ones first.  Results do not depend on
+ * the order.  The per-job records of the finished run are permuted the same
+ * way so that they stay matched with the job table.  Runs with the stream
+ * idle (after the synchronisation in odp_plan_finish), so neither the job
+ * table nor the initial state is being read by the device. */
+static int reorder_by_duration(odp_plan *p)
+{
+  gbx_job_out *jo = (gbx_job_out *)(p->h_state_out + (p->levels_off - p->out_off));
+  unsigned long long t0 = ((const gbx_ctrl *)p->h_state_out)->t_start;
+  for(int k = 0; k < p->njobs; k++){
+    if(jo[k].t_loaded && jo[k].t_loaded < t0) t0 = jo[k].t_loaded;
+    if(jo[k].t_done && jo[k].t_done < t0) t0 = jo[k].t_done;
+  }
+  job_order *ord = malloc(sizeof(job_order) * (size_t)p->njobs);
+  gbx_job *nj = malloc(sizeof(gbx_job) * (size_t)p->njobs);
+  gbx_job_out *no = malloc(sizeof(gbx_job_out) * (size_t)p->njobs);
+  if(!ord || !nj || !no){ free(ord); free(nj); free(no); return ODPX_ERR_MEMORY; }
+  for(int k = 0; k < p->njobs; k++){
+    unsigned long long a = jo[k].t_loaded ? jo[k].t_loaded : t0;
+    ord[k].job = k;
+    ord[k].work = jo[k].t_done > a ? (double)(jo[k].t_done - a) : 0.0;
+  }
+  qsort(ord, (size_t)p->njobs, sizeof(job_order), cmp_work_desc);
+  for(int k = 0; k < p->njobs; k++){
+    nj[k] = p->h_jobs[ord[k].job];
+    no[k] = jo[ord[k].job];
+  }
+  memcpy(p->h_jobs, nj, sizeof(gbx_job) * (size_t)p->njobs);
+  memcpy(jo, no, sizeof(gbx_job_out) * (size_t)p->njobs);
+  free(ord); free(nj); free(no);
+  fill_state_init(p);
+  if(gbx_memcpy_h2d(p->d_jobs, p->h_jobs, sizeof(gbx_job) * (size_t)p->njobs, p->stream)) return ODPX_ERR_CUDA;
+  if(gbx_stream_sync(p->stream)) return ODPX_ERR_CUDA;
+  return 0;
+}
+
 int odp_plan_finish(odp_plan *p, odp_result *results)
 {
   if(gbx_stream_sync(p->stream)) return ODPX_ERR_CUDA;
@@ -561,6 +607,11 @@ int odp_plan_finish(odp_plan *p, odp_result *results)
   unsigned int err = *(const unsigned int *)(p->h_state_out + sizeof(gbx_ctrl)) | ctrl->error;
   if(err & GBX_ERR_TIMEOUT) return ODPX_ERR_TIMEOUT;
   if(err & GBX_ERR_BAD_ADJ) return ODPX_ERR_ADJACENCY;
+  if(p->tuning.reorder && !p->reordered && p->njobs > p->nslots){
+    p->reordered = 1;
+    int e = reorder_by_duration(p);
+    if(e) return e;
+  }
   const gbx_graph_acc *acc = (const gbx_graph_acc *)(p->h_state_out + (p->acc_off - p->out_off));
   p->bytes_alg_last = 0;
   for(int i = 0; i < p->ngraphs; i++){

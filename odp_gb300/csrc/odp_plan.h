@@ -30,6 +30,7 @@ typedef struct {
   int blocks;                  /* persistent grid size; 0 = SMs x occupancy */
   int activity;                /* change tracking: 0 never (default), 1 always, -1 grids only */
   int local_kb_explicit;       /* local_kb was set by the caller: the tuning table does not override it */
+  int reorder;                 /* after the first run, order jobs by their measured duration (1, default) */
 } odp_tuning;
 
 typedef struct {
@@ -66,6 +67,7 @@ typedef struct odp_plan {
   int blocks;
   int any_active;              /* some job tracks changes: launch with the full staging area */
   double bytes_alg_last;       /* algorithmic bytes of the last run (roofline) */
+  int reordered;               /* the job order was learned from a run */
 } odp_plan;
 
 typedef struct {

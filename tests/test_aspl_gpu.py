@@ -341,3 +341,31 @@ def test_change_tracking_on_and_off(golden, activity, monkeypatch):
         b.close()
     finally:
         og.set_tuning()
+
+
+def test_learned_job_order():
+    """After its first run a plan re-sorts its jobs by measured duration; the
+    results, the per-job levels (matched to the new order) and the
+    algorithmic byte count stay the same run after run."""
+    from odp_gb300 import workloads
+    specs = workloads.build_graphs(workloads.batch_shapes(40, first_seed=900, draw_seed=7))
+    og.set_tuning(slots=2, local_kb=1)
+    try:
+        b = og.Batch(specs)
+        first = b.run()
+        lv1 = sorted(b.job_levels().tolist())
+        by1 = b.bytes_alg()
+        for _ in range(2):
+            again = b.run()
+            assert all(same(x, y) for x, y in zip(first, again))
+            assert sorted(b.job_levels().tolist()) == lv1
+            assert b.bytes_alg() == by1
+        g, a, d = b.job_profile()
+        assert np.all(d > 0) and np.all(d >= a)
+        b.close()
+    finally:
+        og.set_tuning()
+    for sp, r in zip(specs, first):
+        o = oracle.aspl(sp.adjacency, nodes=sp.nodes, symmetries=sp.symmetries, grid=sp.grid, width=sp.width,
+                        height=sp.height)
+        assert same(r, o), (sp.nodes, sp.grid, sp.symmetries)
