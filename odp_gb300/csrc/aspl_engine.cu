@@ -462,13 +462,11 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   int cursor = blockIdx.x % nslots;
   unsigned long long idle_since = 0;
   if(blockIdx.x == 0 && threadIdx.x == 0) ctrl->t_start = globaltimer();
-  int pre_slot = -1, pre_tile = 0;      /* thread 0: a ticket taken ahead of time */
 
   for(;;){
     if(threadIdx.x == 0){
       int state = 0, slot = -1, tile = 0;
-      if(pre_slot >= 0){ slot = pre_slot; tile = pre_tile; pre_slot = -1; state = 1; }
-      else if(take_tile(slots, nslots, cursor, slot, tile)) state = 1;
+      if(take_tile(slots, nslots, cursor, slot, tile)) state = 1;
       if(state == 1){
         __threadfence();                               /* acquire the level's inputs */
         gbx_slot *sl = &slots[slot];
@@ -481,12 +479,6 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
         sh_mask0 = vload(&sl->mask0);
         sh_mask1 = vload(&sl->mask1);
         idle_since = 0;
-        /* Take the next ticket now so its round trip overlaps this tile.  Not
-         * for one-tile jobs: their CTA keeps going level after level. */
-        if(sh_job.ntiles > 1){
-          int s2, t2;
-          if(take_tile(slots, nslots, cursor, s2, t2)){ pre_slot = s2; pre_tile = t2; }
-        }
       }
       else{
         if(vload(&ctrl->retired) >= (unsigned)nslots || (vload(&ctrl->error) & GBX_ERR_TIMEOUT)){
@@ -524,20 +516,32 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
       unsigned *Mcur = (level & 1) ? mask1 : mask0;
       const int r0 = tile * jb.tile_rows;
       const int r1 = min(r0 + jb.tile_rows, jb.n);
+      /* Thread 0 asks for the slot's next tile now; the answer is read after
+       * the rows, so its round trip overlaps them.  While this CTA holds a
+       * tile of the level the level cannot close, so a tile obtained here
+       * belongs to the same level and needs no new set-up. */
+      unsigned long long pre = 0;
+      if(threadIdx.x == 0 && jb.ntiles > 1) pre = atomicAdd(&sl->ticket, 1ull);
       unsigned cnt = run_rows(sh_stage, jb, level, X, Y, Mprev, Mcur, r0, r1);
       cnt = __reduce_add_sync(0xffffffffu, cnt);
       if((threadIdx.x & 31) == 0) sh_warp[threadIdx.x >> 5] = cnt;
-      __threadfence();                                 /* release this thread's row writes */
       __syncthreads();
       if(threadIdx.x == 0){
         unsigned long long c_tile = 0;
         for(int w = 0; w < ENGINE_WARPS; w++) c_tile += sh_warp[w];
         atomicAdd(&sl->count, c_tile);
         atomicAdd(&ctrl->tiles, 1ull);
+        /* Releases the CTA's row writes (ordered before this thread by the
+         * barrier) and the ticket request before the done count. */
         __threadfence();
         unsigned old = atomicAdd(&sl->done, 1u);
         int next = 0;
-        if(old + 1 == (unsigned)jb.ntiles){           /* this CTA closes the level */
+        if(jb.ntiles > 1 && (unsigned)pre < (unsigned)(pre >> 32)){
+          next = 1;                                    /* same slot, same level */
+          sh_tile = (int)(unsigned)pre;
+          sh_level = level;
+        }
+        else if(old + 1 == (unsigned)jb.ntiles){      /* this CTA closes the level */
           __threadfence();
           /* level 1 and the full-gather pass count bits set; the pass with
            * change tracking counts bits added */
@@ -552,7 +556,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
             sl->count = 0;
             sl->done = 0;
             sl->level = level + 1;
-            if(jb.ntiles == 1){ next = 1; sh_level = level + 1; }
+            if(jb.ntiles == 1){ next = 1; sh_level = level + 1; sh_tile = 0; }
             else{
               __threadfence();
               atomicExch(&sl->ticket, (unsigned long long)jb.ntiles << 32);
@@ -590,7 +594,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
       __syncthreads();
       const int more = sh_state;
       level = sh_level;
-      tile = 0;
+      tile = sh_tile;
       __syncthreads();
       if(!more) break;
     }
