@@ -161,7 +161,10 @@ int  ODPX_Serve_create(const ODPX_Serve_config *config, ODPX_Server **server);
 /* Uploads a graph (the adjacency stays on the GPU); *handle names it. */
 int  ODPX_Serve_register(ODPX_Server *server, const ODP_Graph *graph, int *handle);
 /* Queues an evaluation of graph `handle` after applying `ndelta` updates to
- * its resident adjacency (they persist).  Returns at once with a request id. */
+ * its resident adjacency (they persist).  Returns at once with a request id.
+ * A delta must name a local row, a slot below that row's degree (its
+ * num_degrees entry, when the graph has one) and a vertex in [0, n);
+ * otherwise nothing is queued and ODPX_ERR_ADJACENCY is returned. */
 int  ODPX_Serve_submit(ODPX_Server *server, int handle, int ndelta, const ODPX_Delta *deltas, long long *request);
 /* Blocks until the request is done; latency_s = submit -> result. */
 int  ODPX_Serve_wait(ODPX_Server *server, long long request, int *diameter, long *sum, double *ASPL,

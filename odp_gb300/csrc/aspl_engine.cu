@@ -131,8 +131,11 @@ __global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int nde
     int *out = e.nbr + (size_t)row * dp;
     const int base = n / e.s;
     const int m = v % base, shift = (v / base) * base;
+    /* Entries that are not neighbours (beyond the vertex's degree, padding,
+     * or out of range, which is also reported) hold the row itself: OR-ing a
+     * row into itself changes nothing, so the gather needs no test. */
     for(int j = 0; j < dp; j++){
-      int nb = -1;
+      int nb = row;
       if(j < deg){
         if(e.grid_s){
           int u = grid_neighbour(e, v, j);
@@ -257,11 +260,13 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
 }
 
 /* Level k >= 2 without change tracking: P_k[v] = P_{k-1}[v] | OR_j
- * P_{k-1}[nbr[v][j]] over all neighbours, every word written.  Eight 16-byte
- * loads per lane are in flight per step (NB neighbours x V vectors).
- * Returns the bits set at this level. */
+ * P_{k-1}[nbr[v][j]] over the d neighbour columns, every word written.
+ * Eight 16-byte loads per lane are in flight per step (NB neighbours x V
+ * vectors).  Columns that hold no neighbour hold the row itself, so only the
+ * step past the last column needs a test.  Returns the bits set at this
+ * level. */
 template <int WC>
-__device__ unsigned rows_levelk_all(const Stage &st, int dp, const unsigned long long *X, unsigned long long *Y,
+__device__ unsigned rows_levelk_all(const Stage &st, int dp, int d, const unsigned long long *X, unsigned long long *Y,
                                     int row0, int nrows)
 {
   typedef RowShape<WC> S;
@@ -277,15 +282,15 @@ __device__ unsigned rows_levelk_all(const Stage &st, int dp, const unsigned long
 #pragma unroll
     for(int k = 0; k < S::V; k++) acc[k] = __ldcg(xr + k * S::G);
     const int *ip = st.idx + r * dp;
-    for(int j = 0; j < dp; j += NB){
+    for(int j = 0; j < d; j += NB){
       uint4 t[NB][S::V];
 #pragma unroll
       for(int i = 0; i < NB; i++){
-        const int idx = (j + i < dp) ? ip[j + i] : -1;
-        const uint4 *nr = Xv + (size_t)(idx < 0 ? 0 : idx) * S::VPR + gl;
+        const bool ok = j + i < d;
+        const uint4 *nr = Xv + (size_t)ip[ok ? j + i : j] * S::VPR + gl;
 #pragma unroll
         for(int k = 0; k < S::V; k++)
-          t[i][k] = (idx >= 0) ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+          t[i][k] = ok ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
       }
 #pragma unroll
       for(int i = 0; i < NB; i++)
@@ -377,7 +382,7 @@ __device__ unsigned run_block(const Stage &st, int dp, const gbx_job &jb, int le
     return jb.srcpos ? rows_level1<WC, true, true>(st, dp, jb, Y, Mcur, row0, nrows)
                      : rows_level1<WC, true, false>(st, dp, jb, Y, Mcur, row0, nrows);
   }
-  if(level > 1) return rows_levelk_all<WC>(st, dp, X, Y, row0, nrows);
+  if(level > 1) return rows_levelk_all<WC>(st, dp, jb.d, X, Y, row0, nrows);
   return jb.srcpos ? rows_level1<WC, false, true>(st, dp, jb, Y, Mcur, row0, nrows)
                    : rows_level1<WC, false, false>(st, dp, jb, Y, Mcur, row0, nrows);
 }
@@ -946,7 +951,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
     gbx_job &j = jobs[k];
     j = gbx_job();
     j.nbr = desc.nbr;
-    j.n = n; j.dp = dp; j.wc_log2 = wl;
+    j.n = n; j.dp = dp; j.d = d; j.wc_log2 = wl;
     j.src0 = k * wc * 64;
     j.nsrc = B - j.src0 < wc * 64 ? B - j.src0 : wc * 64;
     j.sym = s; j.graph = 0;

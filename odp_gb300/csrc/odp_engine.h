@@ -29,7 +29,7 @@ typedef struct {
 
 /* One (graph, column chunk) BFS job: sources [src0, src0 + nsrc). */
 typedef struct {
-  const int *nbr;          /* device int[n][dp] */
+  const int *nbr;          /* device int[n][dp]; an entry that is no neighbour holds the row itself */
   const int *srcpos;       /* device int[n]: row -> source ordinal (-1: not a source), or NULL: row itself */
   int n, dp;
   int wc_log2;             /* words (uint64) per row in this chunk = 1 << wc_log2, 1..7 */
@@ -38,6 +38,7 @@ typedef struct {
   int graph;               /* index into the graph accumulators */
   int tile_rows, ntiles;
   int flags;               /* GBX_JOB_ACTIVE: gather only words that changed at the previous level */
+  int d;                   /* neighbour columns per row; [d, dp) is padding */
 } gbx_job;
 
 #define GBX_JOB_ACTIVE 1

@@ -329,7 +329,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       int wc = 1 << g->wc_log2;
       for(int c = 0; c < g->nchunks; c++, k++){
         gbx_job *j = &jobs[k];
-        j->n = g->n; j->dp = g->dp; j->wc_log2 = g->wc_log2;
+        j->n = g->n; j->dp = g->dp; j->d = g->d; j->wc_log2 = g->wc_log2;
         j->src0 = c * wc * 64;
         j->nsrc = g->B - j->src0 < wc * 64 ? g->B - j->src0 : wc * 64;
         j->sym = g->s; j->graph = i;

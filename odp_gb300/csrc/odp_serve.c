@@ -41,6 +41,7 @@ typedef struct {
   gbx_expand_desc *d_desc;
   int *h_adj;                  /* host mirror of the compact adjacency */
   int *h_itable;               /* grid symmetry: vertex -> row */
+  int *h_rowdeg;               /* num_degrees of the local rows, or NULL (regular) */
   int busy;                    /* part of an in-flight batch */
 } serve_graph;
 
@@ -232,7 +233,7 @@ static int launch_batch(odp_server *s, serve_lane *l)
     for(int c = 0; c < g->nchunks; c++){
       gbx_job *j = &l->h_jobs[njobs++];
       memset(j, 0, sizeof(*j));
-      j->nbr = g->d_nbr; j->n = g->n; j->dp = g->dp; j->wc_log2 = g->wc_log2;
+      j->nbr = g->d_nbr; j->n = g->n; j->dp = g->dp; j->d = g->d; j->wc_log2 = g->wc_log2;
       j->src0 = c * wc * 64;
       j->nsrc = g->B - j->src0 < wc * 64 ? g->B - j->src0 : wc * 64;
       j->sym = g->s; j->graph = nreq; j->tile_rows = g->tile_rows; j->ntiles = g->ntiles;
@@ -422,6 +423,8 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
   e |= gbx_malloc((void **)&g.d_nbr, sizeof(int) * (size_t)n * g.dp);
   e |= gbx_malloc((void **)&g.d_desc, sizeof(gbx_expand_desc));
   if(gr->num_degrees){
+    g.h_rowdeg = malloc(sizeof(int) * (size_t)g.B);
+    memcpy(g.h_rowdeg, gr->num_degrees, sizeof(int) * (size_t)g.B);
     /* per-vertex degrees as the Init variants expand them (odp_plan.c) */
     h_nd = malloc(sizeof(int) * (size_t)n);
     if(!grid_s || sym == 1){
@@ -473,7 +476,7 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
   free(h_nd);
   if(e || h_err){
     gbx_free(g.d_adj); gbx_free(g.d_nbr); gbx_free(g.d_desc); gbx_free(g.d_ndeg); gbx_free(g.d_itable);
-    free(g.h_adj); free(g.h_itable);
+    free(g.h_adj); free(g.h_itable); free(g.h_rowdeg);
     return e ? ODPX_ERR_CUDA : ODPX_ERR_ADJACENCY;
   }
   pthread_mutex_lock(&s->mu);
@@ -499,7 +502,10 @@ int ODPX_Serve_submit(ODPX_Server *s, int handle, int ndelta, const ODPX_Delta *
   }
   for(int k = 0; k < ndelta; k++){
     const ODPX_Delta *dl = &deltas[k];
-    if(dl->row < 0 || dl->row >= g->B || dl->slot < 0 || dl->slot >= g->d || dl->value < 0 || dl->value >= g->n){
+    /* a slot beyond the row's degree holds no edge (the reference ignores
+     * adjacency entries past num_degrees), so a delta may not target it */
+    if(dl->row < 0 || dl->row >= g->B || dl->slot < 0 || dl->slot >= g->d || dl->value < 0 || dl->value >= g->n ||
+       (g->h_rowdeg && dl->slot >= g->h_rowdeg[dl->row])){
       pthread_mutex_unlock(&s->mu);
       return ODPX_ERR_ADJACENCY;
     }
@@ -604,7 +610,7 @@ void ODPX_Serve_destroy(ODPX_Server *s)
   for(int i = 0; i < s->ngraphs; i++){
     serve_graph *g = &s->graphs[i];
     gbx_free(g->d_adj); gbx_free(g->d_nbr); gbx_free(g->d_desc); gbx_free(g->d_ndeg); gbx_free(g->d_itable);
-    free(g->h_adj); free(g->h_itable);
+    free(g->h_adj); free(g->h_itable); free(g->h_rowdeg);
   }
   free(s->graphs);
   for(long long i = 0; i < s->nreqs; i++) free(s->reqs[i].deltas);

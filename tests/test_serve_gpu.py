@@ -110,3 +110,29 @@ def test_admission_and_bad_requests():
     assert ei.value.code == og.ERR_ADJACENCY
     assert same(srv.wait(srv.submit(h))[:3], oracle.aspl(small, nodes=256))
     srv.close()
+
+
+def test_delta_past_a_rows_degree_is_refused():
+    """With num_degrees, slots past a row's degree hold no edge; a delta that
+    targets one is refused, and an accepted delta still matches the graph
+    evaluated alone."""
+    n, d = 512, 6
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=5), d)
+    deg = np.full(n, d, dtype=np.int32)
+    deg[0] = d - 1
+    adj[0, d - 1] = -1
+    srv = og.Server(lanes=1, max_batch=2, max_nodes=1024, memory_mb=32)
+    h = srv.register(og.GraphSpec(adj.copy(), nodes=n, num_degrees=deg))
+    with pytest.raises(og.ODPError) as ei:
+        srv.submit(h, [(0, d - 1, 7)])
+    assert ei.value.code == og.ERR_ADJACENCY
+    host = adj.copy()
+    host[1, 0] = 9
+    got = srv.wait(srv.submit(h, [(1, 0, 9)]))[:3]
+    b = og.Batch([og.GraphSpec(host, nodes=n, num_degrees=deg)])
+    try:
+        assert same(got, b.run()[0])
+    finally:
+        b.close()
+    assert same(got, oracle.aspl(host, nodes=n, num_degrees=deg))
+    srv.close()
