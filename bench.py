@@ -49,6 +49,10 @@ METRIC = "ASPL evals/s, batched vs per-call on 1 GB300 (bit-exact)"
 C2 = dict(nodes=65536, degree=16, seed=2, sha256="d855fb662f9e9557", result=(6, 9346294313))
 WORKLOAD = ("batched: 512 graphs, seeds 100..611, n log-uniform [256, 8192], d in {4..32}, "
             "80% general / 20% grid (length 3-6), s in {1,2,4}")
+# DRAM traffic of one engine_kernel launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture,
+# profiles/engine_kernel_batch.md) on the first 128 graphs of the batch, with that launch's algorithmic
+# bytes.  A full batch launch's traffic is taken as this scaled by algorithmic bytes.
+NCU_DRAM = {"bytes": 827731456.0 + 900297728.0, "bytes_alg": 24803482864.0, "graphs": 128}
 
 
 def parse():
@@ -402,8 +406,11 @@ def run_own(args):
     hbm = float(peaks.get("hbm_gbs", 6800.0))
     l2 = og.measure_l2_read_gbs(48, 40)
     achieved = balg / (ms * 1e-3) / 1e9
+    traffic = NCU_DRAM["bytes"] * balg / NCU_DRAM["bytes_alg"]
     line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                        "traffic": None, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
+                        "traffic": traffic, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
+                        "traffic_source": "ncu DRAM bytes of one launch on the first %d graphs, scaled by algorithmic "
+                                          "bytes" % NCU_DRAM["graphs"],
                         "bytes_alg_per_launch": balg, "l2_read_peak_measured": l2,
                         "frac_of_l2_read_peak": achieved / l2 if l2 > 0 else None}
     line["clocks"] = clk.summary()
