@@ -85,6 +85,7 @@ struct odp_server {
   serve_req *reqs;             /* indexed by request id */
   long long nreqs, cap_reqs, next_pending;
   serve_lane *lanes;
+  double l2_lane_bytes;        /* bitset working set a lane keeps active at once (L2 share) */
   ODPX_Serve_counters stats;
 };
 
@@ -246,7 +247,18 @@ static int launch_batch(odp_server *s, serve_lane *l)
   while(s->next_pending < s->nreqs && s->reqs[s->next_pending].state != 0) s->next_pending++;
   if(nreq == 0) return 0;
 
-  int nslots = njobs < l->nslots ? njobs : l->nslots;
+  /* Active slots: as many leading jobs as fit the lane's share of L2 (at
+   * least one).  Lanes run at the same time, so their bitsets together must
+   * stay L2-resident; the rest of the jobs queue for a free slot. */
+  int nslots = 0;
+  double fp = 0;
+  while(nslots < njobs && nslots < l->nslots){
+    const gbx_job *j = &l->h_jobs[nslots];
+    double f = 16.0 * (double)((size_t)j->n << j->wc_log2);
+    if(nslots > 0 && fp + f > s->l2_lane_bytes) break;
+    fp += f;
+    nslots++;
+  }
   memset(l->h_state, 0, l->state_bytes);
   gbx_slot *sl = (gbx_slot *)l->h_state;
   for(int k = 0; k < nslots; k++){
@@ -366,6 +378,11 @@ int ODPX_Serve_create(const ODPX_Serve_config *cfg, ODPX_Server **out)
   if(per_lane > 256) per_lane = 256;
   int blocks = gbx_engine_blocks(0) / c.lanes;
   if(blocks < 1) blocks = 1;
+  {
+    const char *v = getenv("ODP_GB300_L2_MB");
+    double mb = (v && *v) ? atof(v) : 80.0;
+    s->l2_lane_bytes = mb * 1024.0 * 1024.0 / c.lanes;
+  }
   s->lanes = calloc((size_t)c.lanes, sizeof(serve_lane));
   for(int i = 0; i < c.lanes; i++){
     int e = lane_init(&s->lanes[i], &c, per_lane, blocks);
