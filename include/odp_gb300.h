@@ -10,6 +10,8 @@
  *   ODPX_Batch_*         the same with an explicit, reusable plan
  *   ODPX_Serve_*         device-resident graphs updated by 2-opt deltas,
  *                        evaluated in continuous batches (serving mode)
+ *   ODPX_Anneal_*        simulated-annealing chains whose proposals,
+ *                        evaluations and decisions all run on the GPU
  *   ODPX_Generate_*      the reference generators on a private random stream
  *                        (same graphs for the same seed, thread-safe)
  */
@@ -178,6 +180,53 @@ int  ODPX_Serve_adjacency(ODPX_Server *server, int handle, int *adjacency);
 void ODPX_Serve_destroy(ODPX_Server *server);
 
 /* Library version string. */
+/* ---- Annealing chains on the GPU ----
+ * The reference runs its annealing loop on the host (sample/SA/general.c:
+ * 160-191, general_s.c:170-191): Mutate, Set_aspl, accept_s, Restore when
+ * rejected, temp *= cooling_rate.  ODPX_Anneal runs the same loop for many
+ * chains at once with every step on the GPU: the 2-opt proposal (the
+ * ODP_Mutate_adjacency_general_s rule, drawn from the chain's own stream, the
+ * one ODP_Srand(seed) would give), the evaluation, the acceptance (accept_s:
+ * one more draw from the stream when a move is worse at equal diameter) and
+ * the undo.  A chain given the same seed and temperatures as the reference's
+ * client makes the same moves, except that the acceptance uses the GPU's
+ * exp(), which may differ from the host's in the last bit (a decision can
+ * flip only when the uniform draw falls within that bit).  General(_s)
+ * graphs only. */
+typedef struct {
+  int nodes, degree, symmetries;
+  const int *num_degrees;      /* per local row, or NULL (regular) */
+  const int *adjacency;        /* int[nodes/symmetries][degree]: the starting graph */
+  unsigned int seed;           /* the proposal stream, as ODP_Srand(seed) */
+  double max_temp, min_temp;   /* temperature from max_temp towards min_temp ... */
+  long long ncalcs;            /* ... over ncalcs steps: cooling = pow(min/max, 1/ncalcs) */
+  int hill_climbing;           /* accept only ASPL <= current (the samples' -Y) */
+  int aspl_priority;           /* compare ASPL before diameter (the samples' -A) */
+} ODPX_Chain;
+
+typedef struct {
+  long long steps, accepted;
+  int status;                  /* 0 running; 1 a proposal ran out of draws; 2 an evaluation failed */
+  int diameter;                /* the current graph */
+  long sum;
+  double aspl;
+  int best_diameter;           /* the best graph seen (diameter first, then ASPL) */
+  long best_sum;
+  double best_aspl;
+  double temp;                 /* the next step's temperature */
+} ODPX_Chain_state;
+
+typedef struct odpx_anneal ODPX_Anneal;
+/* Uploads and evaluates the starting graphs (the samples' first Set_aspl). */
+int  ODPX_Anneal_create(const ODPX_Chain *chains, int count, ODPX_Anneal **anneal);
+/* Runs `steps` steps of every chain; returns when they are done. */
+int  ODPX_Anneal_run(ODPX_Anneal *anneal, int steps);
+/* A chain's counters and results, and optionally its current and best
+ * graphs (int[nodes/symmetries][degree] each; NULL to skip). */
+int  ODPX_Anneal_state(ODPX_Anneal *anneal, int chain, ODPX_Chain_state *state, int *adjacency,
+                       int *best_adjacency);
+void ODPX_Anneal_destroy(ODPX_Anneal *anneal);
+
 const char *ODPX_Version(void);
 
 #ifdef __cplusplus

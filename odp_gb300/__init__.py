@@ -585,3 +585,101 @@ def two_opt_deltas(adjacency, restore, nodes, symmetries=1):
             row = vert % base
             out.append((row, slot, int(adjacency[row, slot])))
     return out
+
+
+# --------------------------------------------------------------------------
+# Annealing chains on the GPU (odp_gb300.h ODPX_Anneal_*).
+# --------------------------------------------------------------------------
+
+class ChainC(ctypes.Structure):
+    """ODPX_Chain."""
+    _fields_ = [("nodes", ctypes.c_int), ("degree", ctypes.c_int), ("symmetries", ctypes.c_int),
+                ("num_degrees", ctypes.c_void_p), ("adjacency", ctypes.c_void_p), ("seed", ctypes.c_uint),
+                ("max_temp", ctypes.c_double), ("min_temp", ctypes.c_double), ("ncalcs", ctypes.c_longlong),
+                ("hill_climbing", ctypes.c_int), ("aspl_priority", ctypes.c_int)]
+
+
+class ChainState(ctypes.Structure):
+    """ODPX_Chain_state."""
+    _fields_ = [("steps", ctypes.c_longlong), ("accepted", ctypes.c_longlong), ("status", ctypes.c_int),
+                ("diameter", ctypes.c_int), ("sum", ctypes.c_long), ("aspl", ctypes.c_double),
+                ("best_diameter", ctypes.c_int), ("best_sum", ctypes.c_long), ("best_aspl", ctypes.c_double),
+                ("temp", ctypes.c_double)]
+
+
+def _bind_anneal(lib):
+    if getattr(lib, "_anneal_bound", False):
+        return lib
+    P = ctypes.c_void_p
+    lib.ODPX_Anneal_create.restype = ctypes.c_int
+    lib.ODPX_Anneal_create.argtypes = [ctypes.POINTER(ChainC), ctypes.c_int, ctypes.POINTER(P)]
+    lib.ODPX_Anneal_run.restype = ctypes.c_int
+    lib.ODPX_Anneal_run.argtypes = [P, ctypes.c_int]
+    lib.ODPX_Anneal_state.restype = ctypes.c_int
+    lib.ODPX_Anneal_state.argtypes = [P, ctypes.c_int, ctypes.POINTER(ChainState), P, P]
+    lib.ODPX_Anneal_destroy.restype = None
+    lib.ODPX_Anneal_destroy.argtypes = [P]
+    lib._anneal_bound = True
+    return lib
+
+
+class Chain:
+    """One annealing chain: the starting graph and the client's parameters
+    (seed, max/min temperature over ncalcs steps, -Y hill climbing, -A ASPL
+    priority), as the reference's sample/SA clients take them."""
+
+    def __init__(self, adjacency, nodes, symmetries=1, num_degrees=None, seed=0, max_temp=100.0, min_temp=0.2,
+                 ncalcs=10000, hill_climbing=False, aspl_priority=False):
+        self.adjacency = _ints(adjacency)
+        self.nodes, self.symmetries = nodes, symmetries
+        self.degree = self.adjacency.shape[1]
+        self.num_degrees = None if num_degrees is None else _ints(num_degrees)
+        self.seed, self.max_temp, self.min_temp, self.ncalcs = seed, max_temp, min_temp, ncalcs
+        self.hill_climbing, self.aspl_priority = hill_climbing, aspl_priority
+
+    def to_c(self):
+        return ChainC(self.nodes, self.degree, self.symmetries, _iptr(self.num_degrees), _iptr(self.adjacency),
+                      self.seed, self.max_temp, self.min_temp, self.ncalcs, int(self.hill_climbing),
+                      int(self.aspl_priority))
+
+
+class Anneal:
+    """Annealing chains whose proposals, evaluations and decisions all run on
+    the GPU (ODPX_Anneal_*)."""
+
+    def __init__(self, chains):
+        lib = _bind_anneal(load())
+        self._chains = list(chains)
+        arr = (ChainC * len(self._chains))(*[c.to_c() for c in self._chains])
+        h = ctypes.c_void_p()
+        _check(lib.ODPX_Anneal_create(arr, len(self._chains), ctypes.byref(h)), "ODPX_Anneal_create")
+        self._h = h
+
+    def run(self, steps):
+        _check(load().ODPX_Anneal_run(self._h, steps), "ODPX_Anneal_run")
+
+    def state(self, k, graphs=False):
+        """The chain's counters and results as a dict; with graphs=True also
+        its current and best adjacency."""
+        c = self._chains[k]
+        st = ChainState()
+        cur = best = None
+        if graphs:
+            cur = np.empty_like(c.adjacency)
+            best = np.empty_like(c.adjacency)
+        _check(load().ODPX_Anneal_state(self._h, k, ctypes.byref(st), _iptr(cur), _iptr(best)), "ODPX_Anneal_state")
+        out = {f: getattr(st, f) for f, _ in ChainState._fields_}
+        if graphs:
+            out["adjacency"], out["best_adjacency"] = cur, best
+        return out
+
+    def close(self):
+        if self._h:
+            load().ODPX_Anneal_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

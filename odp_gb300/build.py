@@ -23,8 +23,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc") if os.path.exists(os.path.join(CUDA_HOME, "bin", "nvcc")) else "nvcc"
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
-CU_SOURCES = ["aspl_engine.cu"]
-C_SOURCES = ["odp_graph.c", "odp_io.c", "odp_plan.c", "odp_aspl.c", "odp_batch.c", "odp_serve.c"]
+CU_SOURCES = ["aspl_engine.cu", "anneal.cu"]
+C_SOURCES = ["odp_graph.c", "odp_io.c", "odp_plan.c", "odp_aspl.c", "odp_batch.c", "odp_serve.c", "odp_anneal.c"]
 
 SO_PATH = os.path.join(HERE, "libodp_gb300.so")
 A_PATH = os.path.join(HERE, "libodp_gb300.a")

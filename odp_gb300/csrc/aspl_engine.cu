@@ -717,6 +717,11 @@ int gbx_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream)
   return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream);
 }
 
+int gbx_memcpy_d2d(void *dst, const void *src, size_t bytes, void *stream)
+{
+  return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream);
+}
+
 int gbx_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream)
 {
   return (int)cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream);

@@ -9,6 +9,7 @@
 #define ODP_ENGINE_H
 #include <stddef.h>
 #include <stdint.h>
+#include "odp.h"
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -103,6 +104,7 @@ int  gbx_stream_create(void **stream);
 int  gbx_stream_destroy(void *stream);
 int  gbx_memcpy_h2d(void *dst, const void *src, size_t bytes, void *stream);
 int  gbx_memcpy_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int  gbx_memcpy_d2d(void *dst, const void *src, size_t bytes, void *stream);
 int  gbx_memset(void *dst, int value, size_t bytes, void *stream);
 int  gbx_stream_sync(void *stream);
 const char *gbx_error_string(int err);
@@ -132,6 +134,37 @@ int  gbx_event_create(void **ev);
 int  gbx_event_destroy(void *ev);
 int  gbx_event_record(void *ev, void *stream);
 int  gbx_event_elapsed_ms(void *start, void *stop, float *ms);
+
+/* One simulated-annealing chain on a general(_s) graph, resident on the
+ * device (anneal.cu).  Its graph is evaluated by the engine as graph `graph`
+ * of a plan whose tables `adj` and `nbr` point into. */
+typedef struct {
+  int n, d, dp, s, base, graph;
+  int *adj;                    /* compact int[base][d] */
+  int *nbr;                    /* neighbour table int[n][dp] */
+  const int *ndeg;             /* degree per base row, or NULL (regular) */
+  int *best_adj;               /* int[base][d]: the best graph seen */
+  unsigned int ring[31];       /* proposal stream: the last 31 words of glibc's TYPE_3 recurrence, */
+  int ring_pos;                /*   ring[ring_pos] the oldest */
+  int status;                  /* 0 running, else GBX_CHAIN_ERR_* (the chain stops) */
+  ODP_Restore last;            /* the last swap, for its undo */
+  int cur_diameter, best_diameter;
+  long long cur_sum, best_sum;
+  double cur_aspl, best_aspl;
+  double temp, cooling;        /* temp *= cooling after every step */
+  long long steps, accepted;
+  int hill_climbing, aspl_priority;
+} gbx_chain;
+
+#define GBX_CHAIN_ERR_SWAP 1   /* a proposal found no back slot or ran out of draws */
+#define GBX_CHAIN_ERR_EVAL 2   /* an evaluation reported an error (bad adjacency, timeout) */
+
+/* One proposal per running chain: a 2-opt swap applied to adj and nbr. */
+int  gbx_anneal_propose(gbx_chain *d_chains, int count, void *stream);
+/* One decision per running chain from its evaluation: best tracking (copying
+ * adj to best_adj), acceptance, the undo of a rejected swap, cooling. */
+int  gbx_anneal_decide(gbx_chain *d_chains, int count, const gbx_graph_acc *d_acc, const gbx_ctrl *d_ctrl,
+                       const unsigned int *d_err, void *stream);
 
 #ifdef __cplusplus
 }

@@ -36,11 +36,15 @@
 /* Index arithmetic shared by the general (circulant) and grid symmetries.   */
 /* ------------------------------------------------------------------------ */
 
-typedef struct {              /* a symmetric general graph: n vertices, s orbits */
-  int n, d, s, base;          /* base = n / s rows stored */
-  const int *ndeg;            /* per base row degree, or NULL (regular) */
-  int *adj;                   /* int[base][d] */
-} gen_ctx;
+/* The general (circulant) 2-opt swap is shared with the device annealing
+ * kernels (odp_mutate.h); here it draws from an odp_rng and, like the
+ * reference, retries without a bound. */
+typedef odp_rng mut_rng;
+#define MUT_BELOW(rng, max) odp_rng_below((rng), (max))
+#define MUT_TRIES 0
+#include "odp_mutate.h"
+
+typedef mut_general gen_ctx;  /* a symmetric general graph: n vertices, s orbits */
 
 typedef struct {              /* a (possibly rotation-symmetric) grid graph */
   int w, h, d, s, len, n;
@@ -50,195 +54,22 @@ typedef struct {              /* a (possibly rotation-symmetric) grid graph */
   const int *xy;              /* optional (x, y) per vertex: saves divisions */
 } grid_ctx;
 
-static inline int wrap(int x, int n)            /* NORM, utils.c:171-177 */
-{
-  if(n <= 0) return x;
-  while(x < 0 || x >= n) x = (x < 0) ? x + n : x - n;
-  return x;
-}
+static inline int wrap(int x, int n) { return mut_wrap(x, n); }  /* NORM, utils.c:171-177 */
 
-/* adjacency[v][j] of the expanded general graph (GLOBAL_ADJ_GENERAL, utils.c:180-186) */
-static inline int gen_nbr(const gen_ctx *g, int v, int j)
-{
-  return wrap(g->adj[(size_t)(v % g->base) * g->d + j] + (v / g->base) * g->base, g->n);
-}
-
-/* value to store in row of `pos` so that it names global vertex v (LOCAL_INDEX_GENERAL, utils.c:266-270) */
-static inline int gen_rel(const gen_ctx *g, int v, int pos)
-{
-  return wrap(v - (pos / g->base) * g->base, g->n);
-}
-
-static inline bool gen_is_antipodal(const gen_ctx *g, int u, int v)   /* IS_DIAMETER_GENERAL, utils.c:96-102 */
-{
-  return (g->s % 2 == 0) && abs(u - v) == g->n / 2;
-}
-
-static inline int gen_deg(const gen_ctx *g, int v)
-{
-  return g->ndeg ? g->ndeg[v % g->base] : g->d;
-}
-
-/* The slot of v's row that points back at u (get_degree_index_general, utils.c:509-532). */
-static int gen_back_slot(const gen_ctx *g, int u, int v, int u_slot)
-{
-  if(u == v){
-    int dd = gen_deg(g, v);
-    for(int i = 0; i < dd; i++)
-      if(gen_nbr(g, v, i) == u && i != u_slot) return i;
-  }
-  else if(gen_is_antipodal(g, u, v)){
-    return u_slot;
-  }
-  else{
-    int dd = gen_deg(g, v);
-    for(int i = 0; i < dd; i++)
-      if(gen_nbr(g, v, i) == u) return i;
-  }
-  ODP_FAIL("Something Wrong ! [id=4]\n");
-}
-
-/* Two edges that are images of each other under the rotation (check_rotated_edges_overlap_general, utils.c:603-621). */
-static bool gen_same_orbit(const gen_ctx *g, int u0, int v0, int u1, int v1)
-{
-  int n = g->n;
-  int d0 = (u0 > v0) ? v0 - u0 + n : v0 - u0;
-  int d1 = (u1 > v1) ? v1 - u1 + n : v1 - u1;
-  int d2 = (u1 < v1) ? u1 - v1 + n : u1 - v1;
-  if(d0 == d1 && u0 % g->base == u1 % g->base) return true;
-  if(d0 == d2 && u0 % g->base == v1 % g->base) return true;
-  return false;
-}
-
-static inline void gen_put(gen_ctx *g, int v, int slot, int value)
-{
-  g->adj[(size_t)(v % g->base) * g->d + slot] = value;
-}
+static inline int gen_rel(const gen_ctx *g, int v, int pos) { return mut_rel(g, v, pos); }
 
 static void fill_restore(ODP_Restore *r, const int u[2], const int us[2], const int v[2], const int vs[2])
 {
-  if(!r) return;
-  for(int i = 0; i < 2; i++){
-    r->u[i] = u[i]; r->v[i] = v[i]; r->u_d[i] = us[i]; r->v_d[i] = vs[i];
-  }
+  mut_fill_restore(r, u, us, v, vs);
 }
 
-/* Rotate a single edge to another orbit position (mutate_adjacency_1opt_general_s, utils.c:572-601). */
-static bool gen_one_opt(odp_rng *rng, gen_ctx *g, int u, int us)
-{
-  int base = g->base, s = g->s, n = g->n;
-  int v = gen_nbr(g, u, us);
-  if(gen_is_antipodal(g, u, v)) return false;
-  int vs = gen_back_slot(g, u, v, us);
-  int nv;
-  if((u - v) % base == 0){
-    if(s <= 4) return false;
-    for(;;){
-      nv = v + base * odp_rng_below(rng, s);
-      if(u == nv || v == nv) continue;
-      if(wrap(u - v, n) == wrap(nv - u, n)) continue;
-      if(n % 2 == 1) break;
-      if((u - nv) % (n / 2) != 0) break;
-    }
-  }
-  else{
-    int k = (s % 2 == 1) ? odp_rng_below(rng, s - 1) : odp_rng_below(rng, s);
-    nv = (k != s - 1) ? v + base * (k + 1) : u + base * (s / 2);
-  }
-  int nu = v - (nv - u);
-  int a = gen_rel(g, nv, u), b = gen_rel(g, nu, v);
-  gen_put(g, u, us, a);
-  gen_put(g, v, vs, b);
-  return true;
-}
-
-/* One 2-opt attempt on a general(_s) graph (mutate_adjacency_2opt_general_s, utils.c:623-750).
- * Returns false when the attempt is rejected; the caller retries. */
+/* One 2-opt attempt on a general(_s) graph; false when the attempt is
+ * rejected and the caller retries. */
 static bool gen_two_opt(odp_rng *rng, gen_ctx *g, ODP_Restore *r)
 {
-  int u[2], v[2], us[2], vs[2];
-  const int n = g->n;
-  for(;;){
-    u[0] = odp_rng_below(rng, n);
-    u[1] = odp_rng_below(rng, n);
-    if(u[0] == u[1]) continue;
-    us[0] = odp_rng_below(rng, gen_deg(g, u[0]));
-    v[0] = gen_nbr(g, u[0], us[0]);
-    if(v[0] == u[1]) continue;
-    us[1] = odp_rng_below(rng, gen_deg(g, u[1]));
-    v[1] = gen_nbr(g, u[1], us[1]);
-    if(v[1] == u[0] || v[0] == v[1]) continue;
-    break;
-  }
-  vs[0] = gen_back_slot(g, u[0], v[0], us[0]);
-  vs[1] = gen_back_slot(g, u[1], v[1], us[1]);
-  fill_restore(r, u, us, v, vs);
-
-  bool a0 = gen_is_antipodal(g, u[0], v[0]), a1 = gen_is_antipodal(g, u[1], v[1]);
-  if(a0 && a1){
-    if((u[0] - u[1]) % g->base == 0) return false;
-    int t0, t1;
-    if(odp_rng_below(rng, 2)){ t0 = gen_rel(g, u[1], u[0]); t1 = gen_rel(g, u[0], u[1]); }
-    else                     { t0 = gen_rel(g, v[1], u[0]); t1 = gen_rel(g, v[0], u[1]); }
-    gen_put(g, u[0], us[0], t0);
-    gen_put(g, u[1], us[1], t1);
-    return true;
-  }
-  if(a0 || a1){
-    if(a1){
-      int t;
-      t = u[0]; u[0] = u[1]; u[1] = t;
-      t = us[0]; us[0] = us[1]; us[1] = t;
-      t = v[0]; v[0] = v[1]; v[1] = t;
-      t = vs[0]; vs[0] = vs[1]; vs[1] = t;
-    }
-    int opp = n / 2, k = odp_rng_below(rng, 4), t[4];
-    switch(k){
-    case 0:
-      t[0] = gen_rel(g, v[1], u[0]);        t[1] = gen_rel(g, u[1] + opp, u[1]);
-      t[2] = gen_rel(g, v[1] + opp, v[0]);  t[3] = gen_rel(g, u[0], v[1]);
-      break;
-    case 1:
-      t[0] = gen_rel(g, v[1] + opp, u[0]);  t[1] = gen_rel(g, u[1] + opp, u[1]);
-      t[2] = gen_rel(g, v[1], v[0]);        t[3] = gen_rel(g, v[0], v[1]);
-      break;
-    case 2:
-      t[0] = gen_rel(g, u[1], u[0]);        t[1] = gen_rel(g, u[0], u[1]);
-      t[2] = gen_rel(g, u[1] + opp, v[0]);  t[3] = gen_rel(g, v[1] + opp, v[1]);
-      break;
-    default:
-      t[0] = gen_rel(g, u[1] + opp, u[0]);  t[1] = gen_rel(g, v[0], u[1]);
-      t[2] = gen_rel(g, u[1], v[0]);        t[3] = gen_rel(g, v[1] + opp, v[1]);
-      break;
-    }
-    gen_put(g, u[0], us[0], t[0]);
-    gen_put(g, u[1], us[1], t[1]);
-    gen_put(g, v[0], vs[0], t[2]);
-    gen_put(g, v[1], vs[1], t[3]);
-    return true;
-  }
-
-  if(gen_same_orbit(g, u[0], v[0], u[1], v[1]))
-    return gen_one_opt(rng, g, u[0], us[0]);
-
-  int t[4];
-  if(odp_rng_below(rng, 2)){            /* u0--v1, v0--u1 */
-    if(gen_is_antipodal(g, u[0], v[1]) || gen_is_antipodal(g, v[0], u[1])) return false;
-    if(gen_same_orbit(g, u[0], v[1], v[0], u[1])) return false;
-    t[0] = gen_rel(g, v[1], u[0]); t[1] = gen_rel(g, v[0], u[1]);
-    t[2] = gen_rel(g, u[1], v[0]); t[3] = gen_rel(g, u[0], v[1]);
-  }
-  else{                                 /* u0--u1, v0--v1 */
-    if(gen_is_antipodal(g, u[0], u[1]) || gen_is_antipodal(g, v[0], v[1])) return false;
-    if(gen_same_orbit(g, u[0], u[1], v[0], v[1])) return false;
-    t[0] = gen_rel(g, u[1], u[0]); t[1] = gen_rel(g, u[0], u[1]);
-    t[2] = gen_rel(g, v[1], v[0]); t[3] = gen_rel(g, v[0], v[1]);
-  }
-  gen_put(g, u[0], us[0], t[0]);
-  gen_put(g, u[1], us[1], t[1]);
-  gen_put(g, v[0], vs[0], t[2]);
-  gen_put(g, v[1], vs[1], t[3]);
-  return true;
+  int e = mut_two_opt(rng, g, r);
+  if(e < 0) ODP_FAIL("Something Wrong ! [id=4]\n");
+  return e == 1;
 }
 
 /* ------------------------------------------------------------------------ */
