@@ -68,6 +68,7 @@ def parse():
     p.add_argument("--no-per-call", action="store_true")
     p.add_argument("--cpu-seconds", type=float, default=10.0)
     p.add_argument("--no-serving", action="store_true")
+    p.add_argument("--no-anneal", action="store_true")
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=8.0)
     return p.parse_args()
@@ -287,6 +288,62 @@ def serving(seconds, rate=20000.0):
             "note": "the offered cap exceeds what any GPU can serve for n=32768 chains; chains are closed loop"}
 
 
+def anneal(seconds, temperature=50.0):
+    """The served annealing chains with every step on the GPU (ODPX_Anneal):
+    the same 64 chains, grouped by size into 4 sets of 16 that run
+    concurrently, each on a quarter of the persistent grid, so that small
+    chains do not step at the pace of large ones.  Constant temperature, as
+    the serving leg."""
+    import torch
+    import odp_gb300 as og
+    from odp_gb300 import workloads
+    shapes = workloads.chain_shapes(64)
+    specs = workloads.build_graphs(shapes)
+    sizes = sorted({s["nodes"] for s in shapes})
+    idx = [[i for i, s in enumerate(shapes) if s["nodes"] == n] for n in sizes]
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    os.environ["ODP_GB300_BLOCKS"] = str(max(1, sms * 4 // len(sizes)))
+    try:
+        groups = [og.Anneal([og.Chain(specs[i].adjacency, shapes[i]["nodes"], seed=shapes[i]["proposal_seed"],
+                                      max_temp=temperature, min_temp=temperature, ncalcs=1) for i in g])
+                  for g in idx]
+    finally:
+        del os.environ["ODP_GB300_BLOCKS"]
+    for g in groups:
+        g.run(1)
+    counts = [0] * len(groups)
+    stop = time.perf_counter() + seconds
+
+    def work(k):
+        while time.perf_counter() < stop:
+            groups[k].run(4)
+            counts[k] += 4 * len(idx[k])
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(len(groups))]
+    t0 = time.perf_counter()
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    wall = time.perf_counter() - t0
+    # the reported state is that of the graph each chain holds
+    for g, members in zip(groups, idx):
+        st = g.state(0, graphs=True)
+        sp = specs[members[0]]
+        b = og.Batch([og.GraphSpec(st["adjacency"], nodes=sp.nodes)])
+        assert same(b.run()[0], (st["diameter"], st["sum"], st["aspl"])), "chain state differs from its graph"
+        b.close()
+    accepted = sum(g.state(k)["accepted"] for g, m in zip(groups, idx) for k in range(len(m)))
+    for g in groups:
+        g.close()
+    return {"workload": "the 64 served chains, 2-opt proposal + evaluation + acceptance + undo per step on the GPU, "
+                        "4 size groups of 16 on 4 streams, a quarter of the persistent grid each, temperature %g"
+                        % temperature,
+            "seconds": wall, "evals_per_s": sum(counts) / wall,
+            "per_group_evals_per_s": {str(n): c / wall for n, c in zip(sizes, counts)},
+            "accepted": accepted}
+
+
 def same(a, b):
     return a[0] == b[0] and a[1] == b[1] and float(a[2]).hex() == float(b[2]).hex()
 
@@ -405,6 +462,8 @@ def run_own(args):
 
     if not args.no_serving and world == 1:
         line["serving"] = serving(args.serve_seconds)
+    if not args.no_anneal and world == 1:
+        line["anneal"] = anneal(args.serve_seconds)
 
     peaks, src = measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
