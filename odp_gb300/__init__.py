@@ -340,20 +340,28 @@ class GraphSpec:
         return g
 
 
-_batch_arrays = {}
+_batch_cache = [None]          # (specs, their adjacency and degree arrays, the ODP_Graph array)
+
+
+def _results(d, s, a):
+    return list(zip(d.tolist(), s.tolist(), a.tolist()))
 
 
 def set_aspl_batch(specs):
     """ODP_Set_aspl_batch: list of (diameter, sum, ASPL), one per spec."""
     n = len(specs)
-    # the ODP_Graph array is rebuilt only when a spec or one of its arrays changes
-    key = tuple((id(s), s.adjacency.ctypes.data, 0 if s.num_degrees is None else s.num_degrees.ctypes.data)
-                for s in specs)
-    arr = _batch_arrays.get(key)
-    if arr is None:
-        arr = (Graph * n)(*[s.to_c() for s in specs])
-        _batch_arrays.clear()
-        _batch_arrays[key] = arr
+    # The ODP_Graph array is rebuilt only when a spec or one of its arrays is
+    # replaced (identity checks; the cache holds references, so the arrays
+    # the pointers name stay alive).
+    c = _batch_cache[0]
+    if (c is None or len(c[0]) != n or
+            not all(x is y and x.adjacency is ay and x.num_degrees is dy
+                    for x, y, ay, dy in zip(specs, c[0], c[1], c[2]))):
+        specs = list(specs)
+        c = (specs, [s.adjacency for s in specs], [s.num_degrees for s in specs],
+             (Graph * n)(*[s.to_c() for s in specs]))
+        _batch_cache[0] = c
+    arr = c[3]
     d = np.zeros(n, dtype=np.int32)
     s = np.zeros(n, dtype=np.int64)
     a = np.zeros(n, dtype=np.float64)
@@ -361,7 +369,7 @@ def set_aspl_batch(specs):
                                    s.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
                                    a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     _check(rc, "ODP_Set_aspl_batch")
-    return [(int(d[i]), int(s[i]), float(a[i])) for i in range(n)]
+    return _results(d, s, a)
 
 
 class Batch:
@@ -378,7 +386,12 @@ class Batch:
 
     def _adj_ptrs(self, adjacency=None):
         if adjacency is None:
-            adjacency = [s.adjacency for s in self.specs]
+            # the specs' own arrays: their pointers are taken once
+            if getattr(self, "_own_ptrs", None) is None or any(
+                    x.adjacency is not y for x, y in zip(self.specs, self._own_arrays)):
+                self._own_arrays = [s.adjacency for s in self.specs]
+                self._own_ptrs = (ctypes.c_void_p * self.count)(*[a.ctypes.data for a in self._own_arrays])
+            return self._own_ptrs
         self._keep = [_ints(a) for a in adjacency]
         return (ctypes.c_void_p * self.count)(*[a.ctypes.data for a in self._keep])
 
@@ -391,7 +404,7 @@ class Batch:
                                    s.ctypes.data_as(ctypes.POINTER(ctypes.c_long)),
                                    a.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
         _check(rc, "ODPX_Batch_run")
-        return [(int(d[i]), int(s[i]), float(a[i])) for i in range(n)]
+        return _results(d, s, a)
 
     def time(self, repeats, mode=1, flush_mb=0, adjacency=None):
         """Average device ms per run (CUDA events on the plan's stream)."""

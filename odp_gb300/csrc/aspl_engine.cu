@@ -107,9 +107,31 @@ __device__ int grid_neighbour(const gbx_expand_desc &e, int v, int j)
     else if(y >= bh)      { src_row = grid_base_row(grid_rotate(v, w, h, s, 180), h, s); back = 180; }
     else                  { src_row = grid_base_row(grid_rotate(v, w, h, s, 90), h, s); back = 270; }
   }
-  int a = e.adj[(size_t)src_row * d + j];
+  int a = (e.adj_dev ? e.adj_dev : e.adj)[(size_t)src_row * d + j];
   if(a < 0 || a >= n) return -1;
   return back ? grid_rotate(a, w, h, s, back) : a;
+}
+
+/* One descriptor per blockIdx.y: its compact adjacency, read from host
+ * memory by consecutive threads in 16-byte pieces when both ends are 16-byte
+ * aligned, else in 4-byte pieces. */
+__global__ void pull_kernel(const gbx_expand_desc *__restrict__ descs)
+{
+  const gbx_expand_desc &e = descs[blockIdx.y];
+  if(!e.adj_dev) return;
+  const long long ints = (long long)(e.n / e.s) * e.d;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if(((reinterpret_cast<uintptr_t>(e.adj) | reinterpret_cast<uintptr_t>(e.adj_dev)) & 15) == 0){
+    const int4 *src = reinterpret_cast<const int4 *>(e.adj);
+    int4 *dst = reinterpret_cast<int4 *>(e.adj_dev);
+    const long long q = ints >> 2;
+    for(long long i = t0; i < q; i += stride) dst[i] = src[i];
+    for(long long i = (q << 2) + t0; i < ints; i += stride) e.adj_dev[i] = e.adj[i];
+  }
+  else{
+    for(long long i = t0; i < ints; i += stride) e.adj_dev[i] = e.adj[i];
+  }
 }
 
 __global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int ndesc, long long total,
@@ -143,7 +165,7 @@ __global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int nde
           else nb = e.itable[u];
         }
         else{
-          int a = e.adj[(size_t)m * d + j];
+          int a = (e.adj_dev ? e.adj_dev : e.adj)[(size_t)m * d + j];
           if(a < 0 || a >= n) atomicOr(err, GBX_ERR_BAD_ADJ);
           else{ nb = a + shift; if(nb >= n) nb -= n; }
         }
@@ -630,6 +652,7 @@ __global__ void scatter_kernel(const gbx_write *__restrict__ w, int count)
 }
 
 int g_engine_blocks = 0, g_engine_blocks_active = 0;
+int g_pageable_access = 0;
 
 constexpr size_t STAGE_BYTES_PLAIN = sizeof(int) * IDX_SMEM_INTS;
 constexpr size_t STAGE_BYTES_ACTIVE = sizeof(Stage);
@@ -653,6 +676,16 @@ int gbx_device_init(int *sm_count)
   e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if(e != cudaSuccess) return (int)e;
   if(sm_count) *sm_count = sms;
+  {
+    /* Kernels may read pageable host memory (through the host page tables,
+     * as on Grace systems) only when both attributes say so. */
+    int pageable = 0, host_tables = 0;
+    if(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) pageable = 0;
+    if(cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) != cudaSuccess)
+      host_tables = 0;
+    g_pageable_access = pageable == 1 && host_tables == 1;
+    cudaGetLastError();
+  }
   if(g_engine_blocks == 0){
     int per_sm = 0, per_sm_active = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, STAGE_BYTES_PLAIN);
@@ -667,6 +700,8 @@ int gbx_device_init(int *sm_count)
 }
 
 int gbx_engine_blocks(int active) { return active ? g_engine_blocks_active : g_engine_blocks; }
+
+int gbx_pageable_access(void) { return g_pageable_access; }
 
 int gbx_l2_read_probe(size_t bytes, int reps, double *gbs)
 {
@@ -735,6 +770,13 @@ int gbx_memset(void *dst, int value, size_t bytes, void *stream)
 int gbx_stream_sync(void *stream) { return (int)cudaStreamSynchronize((cudaStream_t)stream); }
 
 const char *gbx_error_string(int err) { return cudaGetErrorString((cudaError_t)err); }
+
+int gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream)
+{
+  if(ndesc <= 0) return 0;
+  pull_kernel<<<dim3(32, (unsigned)ndesc), 256, 0, (cudaStream_t)stream>>>(d_descs);
+  return (int)cudaGetLastError();
+}
 
 int gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices, unsigned int *d_error,
                void *stream)

@@ -78,6 +78,7 @@ int ODPX_Anneal_create(const ODPX_Chain *chains, int count, ODPX_Anneal **out)
   odp_tuning t;
   odp_tuning_defaults(&t, count > 1);
   t.reorder = 0;                      /* the job order is fixed once the steps run on the device */
+  t.direct = 0;                       /* the chains update the plan's device copy of the adjacency */
   if((rc = odp_plan_create(shapes, count, &t, &a->p))) goto fail;
   odp_plan *p = a->p;
   /* the starting graphs' evaluation; it also uploads and expands them */

@@ -17,7 +17,10 @@ extern "C" {
 /* One graph whose compact adjacency is turned into a row-space neighbour
  * table nbr[n][dp]: row r lists the rows of r's neighbours, -1 padded. */
 typedef struct {
-  const int *adj;          /* device int[n/s][d] as passed to ODP_Set_aspl */
+  const int *adj;          /* int[n/s][d] as passed to ODP_Set_aspl: a device copy, or the caller's
+                              host array itself when kernels can read pageable host memory */
+  int *adj_dev;            /* NULL, or the device copy that gbx_pull fills from the host array `adj`
+                              and that expand then reads */
   const int *ndeg;         /* device int[n] per-vertex degree, or NULL (regular) */
   const int *itable;       /* device int[n] vertex -> row (grid symmetry), or NULL */
   int *nbr;                /* device out int[n][dp] */
@@ -112,12 +115,18 @@ const char *gbx_error_string(int err);
 /* Kernels. */
 int  gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices,
                 unsigned int *d_error, void *stream);
-int  gbx_engine_blocks(int active);    /* persistent grid size (SMs x resident CTAs) for the launch's staging size */
+int  gbx_engine_blocks(int active);
+/* 1 when kernels can read pageable host memory directly (after gbx_device_init). */
+int  gbx_pageable_access(void);    /* persistent grid size (SMs x resident CTAs) for the launch's staging size */
 /* Streaming read bandwidth of an L2-resident buffer of `bytes` (GB/s). */
 int  gbx_l2_read_probe(size_t bytes, int reps, double *gbs);
 int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots,
                        gbx_ctrl *d_ctrl, gbx_graph_acc *d_acc, gbx_job_out *d_job_out,
                        unsigned long long spin_limit_ns, int blocks, int active, void *stream);
+
+/* Copies every descriptor's host array `adj` into its `adj_dev` with
+ * coalesced 16-byte loads over the CPU-GPU link (pageable host memory). */
+int  gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream);
 
 /* Applies `count` writes, in stream order. */
 int  gbx_scatter(const gbx_write *d_writes, int count, void *stream);

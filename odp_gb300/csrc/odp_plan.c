@@ -54,6 +54,7 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->activity = env_int("ODP_GB300_ACTIVITY", 0);
   t->local_kb_explicit = getenv("ODP_GB300_LOCAL_KB") != NULL;
   t->reorder = env_int("ODP_GB300_REORDER", 1);
+  t->direct = env_int("ODP_GB300_DIRECT", 1);
 }
 
 static int ilog2_ceil(long long x)
@@ -399,7 +400,9 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   CK(gbx_malloc((void **)&p->d_expand, sizeof(gbx_expand_desc) * (size_t)count));
   CK(gbx_malloc((void **)&p->d_jobs, sizeof(gbx_job) * (size_t)njobs));
   CK(gbx_malloc((void **)&p->d_state, p->state_bytes));
-  CK(gbx_host_alloc((void **)&p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4)));
+  p->direct = tuning->direct && gbx_pageable_access();
+  if(p->direct) CK(gbx_host_alloc((void **)&p->h_expand, sizeof(gbx_expand_desc) * (size_t)count));
+  else CK(gbx_host_alloc((void **)&p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4)));
   CK(gbx_host_alloc((void **)&p->h_state_init, p->state_bytes));
   CK(gbx_host_alloc((void **)&p->h_state_out, p->out_bytes));
 
@@ -439,6 +442,12 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     if(h_nd) CK(gbx_memcpy_h2d(p->d_ndeg, h_nd, sizeof(int) * p->ndeg_ints, p->stream));
     if(h_it) CK(gbx_memcpy_h2d(p->d_itable, h_it, sizeof(int) * p->itable_ints, p->stream));
     CK(gbx_memcpy_h2d(p->d_expand, ed, sizeof(gbx_expand_desc) * (size_t)count, p->stream));
+    if(p->direct){
+      /* per call: `adj` names the caller's host array, `adj_dev` the device
+       * copy that gbx_pull fills and expand reads */
+      memcpy(p->h_expand, ed, sizeof(gbx_expand_desc) * (size_t)count);
+      for(int i = 0; i < count; i++) p->h_expand[i].adj_dev = (int *)ed[i].adj;
+    }
     CK(gbx_memcpy_h2d(p->d_jobs, p->h_jobs, sizeof(gbx_job) * (size_t)njobs, p->stream));
     CK(gbx_stream_sync(p->stream));
     free(h_nd); free(h_it); free(h_sp); free(ed);
@@ -459,7 +468,7 @@ void odp_plan_destroy(odp_plan *p)
   if(p->graph_exec) gbx_graph_destroy(p->graph_exec);
   gbx_free(p->d_adj); gbx_free(p->d_ndeg); gbx_free(p->d_itable); gbx_free(p->d_nbr);
   gbx_free(p->d_slotbuf); gbx_free(p->d_slotmask); gbx_free(p->d_srcpos); gbx_free(p->d_expand); gbx_free(p->d_jobs); gbx_free(p->d_state);
-  gbx_host_free(p->h_adj); gbx_host_free(p->h_state_init); gbx_host_free(p->h_state_out);
+  gbx_host_free(p->h_adj); gbx_host_free(p->h_expand); gbx_host_free(p->h_state_init); gbx_host_free(p->h_state_out);
   if(p->stream) gbx_stream_destroy(p->stream);
   free(p->h_jobs);
   free(p->g);
@@ -470,7 +479,15 @@ void odp_plan_destroy(odp_plan *p)
 static int enqueue(odp_plan *p)
 {
   int e;
-  if((e = gbx_memcpy_h2d(p->d_adj, p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4), p->stream))) return e;
+  if(p->direct){
+    /* the descriptors carry this call's host pointers; the pull kernel copies
+     * the arrays into the device copy that expand reads */
+    if((e = gbx_memcpy_h2d(p->d_expand, p->h_expand, sizeof(gbx_expand_desc) * (size_t)p->ngraphs, p->stream)))
+      return e;
+    if((e = gbx_pull(p->d_expand, p->ngraphs, p->stream))) return e;
+  }
+  else if((e = gbx_memcpy_h2d(p->d_adj, p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4), p->stream)))
+    return e;
   if((e = gbx_memcpy_h2d(p->d_state, p->h_state_init, p->state_bytes, p->stream))) return e;
   if((e = gbx_expand(p->d_expand, p->ngraphs, p->total_vertices,
                      (unsigned int *)(p->d_state + p->out_off + sizeof(gbx_ctrl)), p->stream))) return e;
@@ -507,11 +524,21 @@ static void *stage_worker(void *arg)
   return NULL;
 }
 
-/* Copies the callers' adjacency arrays into the pinned staging buffer that
- * the upload reads.  Large batches are split over host threads by bytes:
- * one thread copies at a fraction of the memory bandwidth. */
+/* Hands this call's adjacency arrays to the device.  When kernels can read
+ * pageable host memory, a pull kernel reads the callers' arrays in place
+ * (coalesced 16-byte loads over the CPU-GPU link) and only their pointers are
+ * recorded here: no host-side copy.  Otherwise the arrays
+ * are copied into the pinned staging buffer that the upload reads; large
+ * batches are split over host threads by bytes, since one thread copies at a
+ * fraction of the memory bandwidth. */
 void odp_plan_stage(odp_plan *p, const int *const *adjacency)
 {
+  if(p->direct){
+    /* The device reads pageable host memory: no staging copy, only the
+     * pointers (the arrays must stay unchanged until the run is finished). */
+    for(int i = 0; i < p->ngraphs; i++) p->h_expand[i].adj = adjacency[i];
+    return;
+  }
   size_t total = sizeof(int) * p->adj_ints;
   long cpus = sysconf(_SC_NPROCESSORS_ONLN);
   int nt = total < (4u << 20) ? 1 : (int)(cpus < 16 ? cpus : 16);

@@ -31,6 +31,7 @@ typedef struct {
   int activity;                /* change tracking: 0 never (default), 1 always, -1 grids only */
   int local_kb_explicit;       /* local_kb was set by the caller: the tuning table does not override it */
   int reorder;                 /* after the first run, order jobs by their measured duration (1, default) */
+  int direct;                  /* pull callers' adjacency from host memory when the device can (1, default) */
 } odp_tuning;
 
 typedef struct {
@@ -68,6 +69,8 @@ typedef struct odp_plan {
   int any_active;              /* some job tracks changes: launch with the full staging area */
   double bytes_alg_last;       /* algorithmic bytes of the last run (roofline) */
   int reordered;               /* the job order was learned from a run */
+  int direct;                  /* the device pulls the callers' arrays (h_expand holds their pointers) */
+  gbx_expand_desc *h_expand;   /* pinned copy of the expand descriptors (direct plans) */
 } odp_plan;
 
 typedef struct {

@@ -369,3 +369,35 @@ def test_learned_job_order():
         o = oracle.aspl(sp.adjacency, nodes=sp.nodes, symmetries=sp.symmetries, grid=sp.grid, width=sp.width,
                         height=sp.height)
         assert same(r, o), (sp.nodes, sp.grid, sp.symmetries)
+
+
+def test_staged_and_direct_adjacency_give_the_same_results(monkeypatch):
+    """Plans read callers' arrays in place when the device can read pageable
+    host memory, else through a pinned staging copy; both paths agree with
+    each other and with the oracle, run after run with changing arrays."""
+    from odp_gb300 import workloads
+    specs = workloads.build_graphs(workloads.batch_shapes(24, first_seed=700, draw_seed=11))
+    out = {}
+    for mode in ("1", "0"):
+        monkeypatch.setenv("ODP_GB300_DIRECT", mode)
+        b = og.Batch(specs)
+        try:
+            first = b.run()
+            other = [s.adjacency.copy() for s in specs]
+            rng = og.Rng(5)
+            for k, s in enumerate(specs):           # a few 2-opt swaps on every general graph
+                if not s.grid:
+                    for _ in range(3):
+                        rng.mutate_general(s.nodes, s.degree, other[k], symmetries=s.symmetries)
+            second = b.run(other)
+            third = b.run()
+        finally:
+            b.close()
+        assert all(same(x, y) for x, y in zip(first, third))
+        out[mode] = (first, second)
+    assert all(same(x, y) for x, y in zip(out["1"][0], out["0"][0]))
+    assert all(same(x, y) for x, y in zip(out["1"][1], out["0"][1]))
+    for sp, r in zip(specs[:8], out["1"][0]):
+        o = oracle.aspl(sp.adjacency, nodes=sp.nodes, symmetries=sp.symmetries, grid=sp.grid, width=sp.width,
+                        height=sp.height)
+        assert same(r, o)
