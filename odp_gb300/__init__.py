@@ -110,6 +110,11 @@ def load():
         "ODPX_Mutate_adjacency_general_s_rng": (None, [P, I, I, P, I, ctypes.POINTER(Restore), P]),
         "ODPX_Restore_adjacency_general_s": (None, [I, I, I, Restore, P]),
         "ODPX_Version": (ctypes.c_char_p, []),
+        "ODP_Get_lines": (I, [ctypes.c_char_p]),
+        "ODP_Read_edge_general": (None, [ctypes.c_char_p, P]),
+        "ODP_Read_edge_grid": (None, [ctypes.c_char_p, IP, IP, P]),
+        "ODP_Write_edge_general": (None, [I, P, ctypes.c_char_p]),
+        "ODP_Write_edge_grid": (None, [I, I, P, ctypes.c_char_p]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)
@@ -230,6 +235,38 @@ def conv_edge2adjacency_general(nodes, edge, degree, symmetries=1):
     adj = np.zeros((nodes // symmetries, degree), dtype=np.int32)
     load().ODP_Conv_edge2adjacency_general_s(nodes, len(edge), degree, _iptr(edge), symmetries, _iptr(adj))
     return adj
+
+
+def get_lines(fname):
+    """ODP_Get_lines: newline characters in the file."""
+    return int(load().ODP_Get_lines(os.fsencode(fname)))
+
+
+def read_edge_general(fname):
+    """ODP_Read_edge_general: int32[lines][2] (lines = ODP_Get_lines)."""
+    lines = get_lines(fname)
+    edge = np.zeros((max(lines, 1), 2), dtype=np.int32)
+    load().ODP_Read_edge_general(os.fsencode(fname), _iptr(edge))
+    return edge[:lines]
+
+
+def read_edge_grid(fname):
+    """ODP_Read_edge_grid: (width, height, int32[lines][2])."""
+    lines = get_lines(fname)
+    edge = np.zeros((max(lines, 1), 2), dtype=np.int32)
+    w, h = ctypes.c_int(), ctypes.c_int()
+    load().ODP_Read_edge_grid(os.fsencode(fname), ctypes.byref(w), ctypes.byref(h), _iptr(edge))
+    return w.value, h.value, edge[:lines]
+
+
+def write_edge_general(edge, fname):
+    edge = _ints(edge)
+    load().ODP_Write_edge_general(len(edge), _iptr(edge), os.fsencode(fname))
+
+
+def write_edge_grid(edge, height, fname):
+    edge = _ints(edge)
+    load().ODP_Write_edge_grid(len(edge), height, _iptr(edge), os.fsencode(fname))
 
 
 def conv_edge2adjacency_grid(width, height, edge, degree, symmetries=1):

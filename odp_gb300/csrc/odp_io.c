@@ -10,6 +10,9 @@
 #include <stdlib.h>
 #include <stdbool.h>
 #include <math.h>
+#include <string.h>
+#include <pthread.h>
+#include <unistd.h>
 #include "odp.h"
 
 #define FAIL(...) do{ fprintf(stderr, __VA_ARGS__); exit(1); }while(0)
@@ -83,16 +86,23 @@ void ODP_Set_degrees(int nodes, int lines, int (*edge)[2], int *num_degrees)
   }
 }
 
-/* ODP_Get_lines, utils.c:1369-1384: number of newline characters. */
+/* ODP_Get_lines, utils.c:1369-1384: number of newline characters (counted
+ * a block at a time). */
 int ODP_Get_lines(char *fname)
 {
   FILE *fp = fopen(fname, "r");
   if(!fp) FAIL("File not found\n");
-  int lines = 0, c;
-  while((c = fgetc(fp)) != EOF)
-    if(c == '\n') lines++;
+  enum { BLOCK = 1 << 20 };
+  char *buf = malloc(BLOCK);
+  long long lines = 0;
+  size_t got;
+  while((got = fread(buf, 1, BLOCK, fp)) > 0){
+    const char *q = buf, *end = buf + got;
+    while((q = memchr(q, '\n', (size_t)(end - q))) != NULL){ lines++; q++; }
+  }
+  free(buf);
   fclose(fp);
-  return lines;
+  return (int)lines;
 }
 
 /* ODP_Get_nodes, utils.c:1358-1367 */
@@ -164,62 +174,254 @@ bool ODP_Check_loop(int lines, int (*edge)[2])
   return false;
 }
 
+/* ------------------------------------------------------------------------ */
+/* Edge files.  The reference reads them with fscanf (utils.c:1386-1429), at  */
+/* tens of MB/s; a graphgolf file of 10^6 vertices is hundreds of MB.  Here   */
+/* the file is read whole and its integers are parsed by hand, in parallel    */
+/* slices cut at newlines, with the conversion rules of %d (skip white space, */
+/* optional sign, decimal digits).  On well-formed files the result is the    */
+/* reference's; the reference loops until fscanf returns EOF, so an odd       */
+/* integer at the end still makes one last edge whose second end is the      */
+/* previous edge's, and so it is here.  A token that is not an integer ends   */
+/* the read (where the reference would loop for ever).                        */
+/* ------------------------------------------------------------------------ */
+
+static char *read_whole(const char *fname, size_t *size)
+{
+  FILE *fp = fopen(fname, "rb");
+  if(!fp) FAIL("File not found\n");
+  if(fseek(fp, 0, SEEK_END) != 0) FAIL("Cannot read %s\n", fname);
+  long len = ftell(fp);
+  if(len < 0 || fseek(fp, 0, SEEK_SET) != 0) FAIL("Cannot read %s\n", fname);
+  char *buf = malloc((size_t)len + 1);
+  if(!buf) FAIL("Out of memory reading %s\n", fname);
+  size_t got = fread(buf, 1, (size_t)len, fp);
+  fclose(fp);
+  buf[got] = '\0';
+  *size = got;
+  return buf;
+}
+
+static inline int is_ws(char c) { return c == ' ' || c == '\t' || c == '\n' || c == '\v' || c == '\f' || c == '\r'; }
+
+/* Next %d integer in [p, end): 1 and *v on success, 0 at the end, -1 on a
+ * token that is not an integer.  *pp moves past what was read. */
+static inline int scan_int(const char **pp, const char *end, int *v)
+{
+  const char *p = *pp;
+  while(p < end && is_ws(*p)) p++;
+  if(p == end){ *pp = p; return 0; }
+  int neg = 0;
+  if(*p == '+' || *p == '-'){ neg = *p == '-'; p++; }
+  if(p == end || *p < '0' || *p > '9'){ *pp = p; return -1; }
+  long long x = 0;
+  while(p < end && *p >= '0' && *p <= '9'){ x = x * 10 + (*p - '0'); p++; }
+  *v = (int)(neg ? -x : x);
+  *pp = p;
+  return 1;
+}
+
+typedef struct {
+  const char *begin, *end;
+  long long count;            /* integers before the slice's end or its first bad token */
+  int bad;                    /* the slice holds a token that is not an integer */
+  long long first;            /* global index of the slice's first integer (pass 2) */
+  long long limit;            /* integers to store in total */
+  int *out;
+} int_slice;
+
+static void *count_ints(void *arg)
+{
+  int_slice *s = arg;
+  const char *p = s->begin;
+  int v, r;
+  s->count = 0;
+  s->bad = 0;
+  while((r = scan_int(&p, s->end, &v)) == 1) s->count++;
+  if(r < 0) s->bad = 1;
+  return NULL;
+}
+
+static void *store_ints(void *arg)
+{
+  int_slice *s = arg;
+  const char *p = s->begin;
+  long long g = s->first;
+  int v;
+  while(g < s->limit && scan_int(&p, s->end, &v) == 1) s->out[g++] = v;
+  return NULL;
+}
+
+/* All integers of buf in order (up to the first bad token) into out (at most
+ * `cap` of them, cap < 0: no limit); returns how many the file has. */
+static long long parse_ints(const char *buf, size_t size, int *out, long long cap)
+{
+  long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+  int nt = size < (4u << 20) ? 1 : (int)(cpus < 16 ? (cpus < 1 ? 1 : cpus) : 16);
+  int_slice sl[16];
+  pthread_t th[16];
+  const char *end = buf + size, *b = buf;
+  for(int k = 0; k < nt; k++){
+    const char *e = (k == nt - 1) ? end : buf + size / (size_t)nt * (size_t)(k + 1);
+    if(e < b) e = b;
+    while(e < end && *e != '\n') e++;            /* slices end after a newline: no token is cut */
+    if(e < end) e++;
+    sl[k].begin = b; sl[k].end = e;
+    b = e;
+  }
+  for(int k = 1; k < nt; k++) if(pthread_create(&th[k], NULL, count_ints, &sl[k])) count_ints(&sl[k]), th[k] = 0;
+  count_ints(&sl[0]);
+  for(int k = 1; k < nt; k++) if(th[k]) pthread_join(th[k], NULL);
+  long long total = 0;
+  int last = nt - 1;
+  for(int k = 0; k < nt; k++){
+    sl[k].first = total;
+    total += sl[k].count;
+    if(sl[k].bad){ last = k; break; }
+  }
+  for(int k = 0; k <= last; k++){ sl[k].limit = (cap < 0 || total < cap) ? total : cap; sl[k].out = out; }
+  for(int k = 1; k <= last; k++) if(pthread_create(&th[k], NULL, store_ints, &sl[k])) store_ints(&sl[k]), th[k] = 0;
+  store_ints(&sl[0]);
+  for(int k = 1; k <= last; k++) if(th[k]) pthread_join(th[k], NULL);
+  return total;
+}
+
 /* ODP_Read_edge_general, utils.c:1386-1401 */
 void ODP_Read_edge_general(char *fname, int (*edge)[2])
 {
-  FILE *fp = fopen(fname, "r");
-  if(!fp) FAIL("File not found\n");
-  int a, b, i = 0;
-  while(fscanf(fp, "%d %d", &a, &b) == 2){
-    edge[i][0] = a;
-    edge[i][1] = b;
-    i++;
+  size_t size;
+  char *buf = read_whole(fname, &size);
+  /* the integers go straight into edge, in file order, as the reference
+   * stores them pair by pair (edge was sized by the caller) */
+  int *flat = &edge[0][0];
+  long long total = parse_ints(buf, size, flat, -1);
+  if(total % 2) flat[total] = total >= 3 ? flat[total - 2] : 0;
+  free(buf);
+}
+
+/* One "x,y x,y" record (the format "%d,%d %d,%d"): 1, 0 at the end, -1 on a
+ * mismatch. */
+static int scan_grid_record(const char **pp, const char *end, int c[4])
+{
+  const char *p = *pp;
+  int r = scan_int(&p, end, &c[0]);
+  if(r <= 0){ *pp = p; return r; }
+  for(int k = 1; k < 4; k++){
+    if(k != 2){                                  /* a literal ',' right after the integer */
+      if(p == end || *p != ',') { *pp = p; return -1; }
+      p++;
+    }
+    if(scan_int(&p, end, &c[k]) != 1){ *pp = p; return -1; }
   }
-  fclose(fp);
+  *pp = p;
+  return 1;
 }
 
 /* ODP_Read_edge_grid, utils.c:1403-1429: "x,y x,y" lines, vertex = x*height + y. */
 void ODP_Read_edge_grid(char *fname, int *w, int *h, int (*edge)[2])
 {
-  FILE *fp = fopen(fname, "r");
-  if(!fp) FAIL("File not found\n");
+  size_t size;
+  char *buf = read_whole(fname, &size);
+  const char *p = buf, *end = buf + size;
   int c[4];
-  *w = 0;
-  *h = 0;
-  while(fscanf(fp, "%d,%d %d,%d", &c[0], &c[1], &c[2], &c[3]) == 4){
-    *w = max_i(*w, max_i(c[0], c[2]));
-    *h = max_i(*h, max_i(c[1], c[3]));
+  long long rec = 0;
+  int mw = 0, mh = 0;
+  while(scan_grid_record(&p, end, c) == 1){
+    if(c[0] > mw) mw = c[0];
+    if(c[2] > mw) mw = c[2];
+    if(c[1] > mh) mh = c[1];
+    if(c[3] > mh) mh = c[3];
+    rec++;
   }
-  *w += 1;
-  *h += 1;
-  rewind(fp);
-  int i = 0;
-  while(fscanf(fp, "%d,%d %d,%d", &c[0], &c[1], &c[2], &c[3]) == 4){
+  *w = mw + 1;
+  *h = mh + 1;
+  p = buf;
+  for(long long i = 0; i < rec && scan_grid_record(&p, end, c) == 1; i++){
     edge[i][0] = c[0] * (*h) + c[1];
     edge[i][1] = c[2] * (*h) + c[3];
-    i++;
+  }
+  free(buf);
+}
+
+/* Writers: the same text as the reference's fprintf loops, formatted by hand
+ * in parallel slices and written in order. */
+static inline char *put_int(char *o, int v)
+{
+  char t[12];
+  int n = 0;
+  unsigned u = v < 0 ? 0u - (unsigned)v : (unsigned)v;
+  do{ t[n++] = (char)('0' + u % 10); u /= 10; }while(u);
+  if(v < 0) *o++ = '-';
+  while(n) *o++ = t[--n];
+  return o;
+}
+
+typedef struct {
+  const int (*edge)[2];
+  int first, last, height;      /* height > 0: grid text */
+  char *text;
+  size_t len;
+} text_slice;
+
+static void *format_edges(void *arg)
+{
+  text_slice *s = arg;
+  char *o = s->text;
+  for(int i = s->first; i < s->last; i++){
+    if(s->height > 0){
+      const int h = s->height;
+      o = put_int(o, s->edge[i][0] / h); *o++ = ',';
+      o = put_int(o, s->edge[i][0] % h); *o++ = ' ';
+      o = put_int(o, s->edge[i][1] / h); *o++ = ',';
+      o = put_int(o, s->edge[i][1] % h); *o++ = '\n';
+    }
+    else{
+      o = put_int(o, s->edge[i][0]); *o++ = ' ';
+      o = put_int(o, s->edge[i][1]); *o++ = '\n';
+    }
+  }
+  s->len = (size_t)(o - s->text);
+  return NULL;
+}
+
+static void write_edges(int lines, int height, int (*edge)[2], const char *fname)
+{
+  FILE *fp = fopen(fname, "w");
+  if(!fp) FAIL("Cannot open %s\n", fname);
+  long cpus = sysconf(_SC_NPROCESSORS_ONLN);
+  int nt = lines < (1 << 18) ? 1 : (int)(cpus < 16 ? (cpus < 1 ? 1 : cpus) : 16);
+  const size_t per_line = height > 0 ? 48 : 24;
+  text_slice sl[16];
+  pthread_t th[16];
+  for(int k = 0; k < nt; k++){
+    sl[k].edge = (const int (*)[2])edge;
+    sl[k].first = (int)((long long)lines * k / nt);
+    sl[k].last = (int)((long long)lines * (k + 1) / nt);
+    sl[k].height = height;
+    sl[k].text = malloc(per_line * (size_t)(sl[k].last - sl[k].first) + 1);
+    if(!sl[k].text) FAIL("Out of memory writing %s\n", fname);
+  }
+  for(int k = 1; k < nt; k++) if(pthread_create(&th[k], NULL, format_edges, &sl[k])) format_edges(&sl[k]), th[k] = 0;
+  format_edges(&sl[0]);
+  for(int k = 1; k < nt; k++) if(th[k]) pthread_join(th[k], NULL);
+  for(int k = 0; k < nt; k++){
+    if(fwrite(sl[k].text, 1, sl[k].len, fp) != sl[k].len) FAIL("Cannot write %s\n", fname);
+    free(sl[k].text);
   }
   fclose(fp);
 }
 
-/* ODP_Write_edge_general, utils.c:1153-1164 */
+/* ODP_Write_edge_general, utils.c:1153-1164: "%d %d\n" per edge */
 void ODP_Write_edge_general(int lines, int (*edge)[2], char *fname)
 {
-  FILE *fp = fopen(fname, "w");
-  if(!fp) FAIL("Cannot open %s\n", fname);
-  for(int i = 0; i < lines; i++) fprintf(fp, "%d %d\n", edge[i][0], edge[i][1]);
-  fclose(fp);
+  write_edges(lines, 0, edge, fname);
 }
 
-/* ODP_Write_edge_grid, utils.c:1166-1180 */
+/* ODP_Write_edge_grid, utils.c:1166-1180: "%d,%d %d,%d\n" per edge */
 void ODP_Write_edge_grid(int lines, int height, int (*edge)[2], char *fname)
 {
-  FILE *fp = fopen(fname, "w");
-  if(!fp) FAIL("Cannot open %s\n", fname);
-  for(int i = 0; i < lines; i++)
-    fprintf(fp, "%d,%d %d,%d\n", edge[i][0] / height, edge[i][0] % height, edge[i][1] / height,
-            edge[i][1] % height);
-  fclose(fp);
+  if(height <= 0) FAIL("height must be positive\n");
+  write_edges(lines, height, edge, fname);
 }
 
 /* ODP_Print_adjacency, utils.c:25-38 */
