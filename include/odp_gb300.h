@@ -117,6 +117,10 @@ void   ODPX_Mutate_adjacency_general_s_rng(void *rng_state, int nodes, int degre
                                            int symmetries, ODP_Restore *r, int *adjacency);
 /* ODP_Restore_adjacency_general with the graph's shape given explicitly. */
 void   ODPX_Restore_adjacency_general_s(int nodes, int degree, int symmetries, ODP_Restore r, int *adjacency);
+/* The same two for grids (ODP_Mutate_adjacency_grid_s, ODP_Restore_adjacency_grid). */
+void   ODPX_Mutate_adjacency_grid_s_rng(void *rng_state, int width, int height, int degree, const int *num_degrees,
+                                        int length, int symmetries, ODP_Restore *r, int *adjacency);
+void   ODPX_Restore_adjacency_grid_s(int width, int height, int degree, int symmetries, ODP_Restore r, int *adjacency);
 
 /* ODPX_Set_aspl_noalloc: no counterpart in the reference.  Evaluates one
  * regular general graph (the arguments of ODP_Init_aspl_general[_s] with
@@ -191,8 +195,9 @@ void ODPX_Serve_destroy(ODPX_Server *server);
  * the undo.  A chain given the same seed and temperatures as the reference's
  * client makes the same moves, except that the acceptance uses the GPU's
  * exp(), which may differ from the host's in the last bit (a decision can
- * flip only when the uniform draw falls within that bit).  General(_s)
- * graphs only. */
+ * flip only when the uniform draw falls within that bit).  General(_s) and
+ * grid(_s) graphs (sample/SA/grid.c, grid_s.c: ODP_Mutate_adjacency_grid_s
+ * with its length limit). */
 typedef struct {
   int nodes, degree, symmetries;
   const int *num_degrees;      /* per local row, or NULL (regular) */
@@ -202,6 +207,8 @@ typedef struct {
   long long ncalcs;            /* ... over ncalcs steps: cooling = pow(min/max, 1/ncalcs) */
   int hill_climbing;           /* accept only ASPL <= current (the samples' -Y) */
   int aspl_priority;           /* compare ASPL before diameter (the samples' -A) */
+  int grid;                    /* 1: a grid graph of width x height (nodes is ignored) ... */
+  int width, height, length;   /* ... with edges at most `length` long (the grid samples' -L) */
 } ODPX_Chain;
 
 typedef struct {

@@ -109,6 +109,8 @@ def load():
         "ODPX_Rng_next": (I, [P]),
         "ODPX_Mutate_adjacency_general_s_rng": (None, [P, I, I, P, I, ctypes.POINTER(Restore), P]),
         "ODPX_Restore_adjacency_general_s": (None, [I, I, I, Restore, P]),
+        "ODPX_Mutate_adjacency_grid_s_rng": (None, [P, I, I, I, P, I, I, ctypes.POINTER(Restore), P]),
+        "ODPX_Restore_adjacency_grid_s": (None, [I, I, I, I, Restore, P]),
         "ODPX_Version": (ctypes.c_char_p, []),
         "ODP_Get_lines": (I, [ctypes.c_char_p]),
         "ODP_Read_edge_general": (None, [ctypes.c_char_p, P]),
@@ -345,6 +347,18 @@ class Rng:
     def restore_general(nodes, degree, r, adjacency, symmetries=1):
         """Undoes a swap of mutate_general (the shape is given explicitly)."""
         load().ODPX_Restore_adjacency_general_s(nodes, degree, symmetries, r, _iptr(adjacency))
+
+    def mutate_grid(self, width, height, degree, length, adjacency, symmetries=1, num_degrees=None):
+        r = Restore()
+        nd = None if num_degrees is None else _ints(num_degrees)
+        load().ODPX_Mutate_adjacency_grid_s_rng(self._buf, width, height, degree, _iptr(nd), length, symmetries,
+                                                ctypes.byref(r), _iptr(adjacency))
+        return r
+
+    @staticmethod
+    def restore_grid(width, height, degree, r, adjacency, symmetries=1):
+        """Undoes a swap of mutate_grid."""
+        load().ODPX_Restore_adjacency_grid_s(width, height, degree, symmetries, r, _iptr(adjacency))
 
 
 # --------------------------------------------------------------------------
@@ -646,7 +660,8 @@ class ChainC(ctypes.Structure):
     _fields_ = [("nodes", ctypes.c_int), ("degree", ctypes.c_int), ("symmetries", ctypes.c_int),
                 ("num_degrees", ctypes.c_void_p), ("adjacency", ctypes.c_void_p), ("seed", ctypes.c_uint),
                 ("max_temp", ctypes.c_double), ("min_temp", ctypes.c_double), ("ncalcs", ctypes.c_longlong),
-                ("hill_climbing", ctypes.c_int), ("aspl_priority", ctypes.c_int)]
+                ("hill_climbing", ctypes.c_int), ("aspl_priority", ctypes.c_int), ("grid", ctypes.c_int),
+                ("width", ctypes.c_int), ("height", ctypes.c_int), ("length", ctypes.c_int)]
 
 
 class ChainState(ctypes.Structure):
@@ -678,10 +693,12 @@ class Chain:
     (seed, max/min temperature over ncalcs steps, -Y hill climbing, -A ASPL
     priority), as the reference's sample/SA clients take them."""
 
-    def __init__(self, adjacency, nodes, symmetries=1, num_degrees=None, seed=0, max_temp=100.0, min_temp=0.2,
-                 ncalcs=10000, hill_climbing=False, aspl_priority=False):
+    def __init__(self, adjacency, nodes=0, symmetries=1, num_degrees=None, seed=0, max_temp=100.0, min_temp=0.2,
+                 ncalcs=10000, hill_climbing=False, aspl_priority=False, grid=False, width=0, height=0, length=0):
         self.adjacency = _ints(adjacency)
-        self.nodes, self.symmetries = nodes, symmetries
+        self.grid, self.width, self.height, self.length = bool(grid), width, height, length
+        self.nodes = width * height if grid else nodes
+        self.symmetries = symmetries
         self.degree = self.adjacency.shape[1]
         self.num_degrees = None if num_degrees is None else _ints(num_degrees)
         self.seed, self.max_temp, self.min_temp, self.ncalcs = seed, max_temp, min_temp, ncalcs
@@ -690,7 +707,7 @@ class Chain:
     def to_c(self):
         return ChainC(self.nodes, self.degree, self.symmetries, _iptr(self.num_degrees), _iptr(self.adjacency),
                       self.seed, self.max_temp, self.min_temp, self.ncalcs, int(self.hill_climbing),
-                      int(self.aspl_priority))
+                      int(self.aspl_priority), int(self.grid), self.width, self.height, self.length)
 
 
 class Anneal:

@@ -2,7 +2,8 @@
  * anneal.cu -- simulated-annealing chains that live on the GPU.
  *
  * The reference's annealing clients (sample/SA/general.c:160-191,
- * general_s.c:170-191) loop on the host: ODP_Mutate_adjacency_general_s,
+ * general_s.c:170-191, grid.c:170-191, grid_s.c:180-201) loop on the host:
+ * ODP_Mutate_adjacency_general_s (or _grid_s),
  * ODP_Set_aspl (which uploads the whole adjacency), then accept_s
  * (sample/SA/common.c:15-37) and ODP_Restore_adjacency_general when the move
  * is rejected, then temp *= cooling_rate.  Here every part of that step runs
@@ -93,6 +94,42 @@ __device__ __forceinline__ mut_general chain_graph(const gbx_chain &c)
   return g;
 }
 
+__device__ __forceinline__ mut_grid chain_grid(const gbx_chain &c)
+{
+  mut_grid g;
+  g.w = c.width; g.h = c.height; g.d = c.d; g.s = c.s; g.len = c.len; g.n = c.n;
+  g.bw = c.width / 2; g.bh = (c.s == 2) ? c.height : c.height / 2;
+  g.ndeg = c.ndeg; g.adj = c.adj; g.xy = nullptr; g.nw = 0;
+  return g;
+}
+
+/* The same for a grid chain.  Without symmetry a row is its vertex.  With
+ * symmetry s (2 or 4) local row m stores base vertex bv (the inverse of
+ * ODP_LOCAL_INDEX_GRID); the orbit member rotated by t steps is vertex
+ * rot(bv), its neighbour rot(a), and the table indexes both through itable,
+ * as expand_kernel builds it. */
+__device__ void apply_to_nbr_grid(const gbx_chain &c, const mut_grid &g)
+{
+  for(int k = 0; k < g.nw; k++){
+    const int m = g.wrow[k], slot = g.wslot[k];
+    const int a = c.adj[(long long)m * c.d + slot];
+    if(c.s == 1){
+      c.nbr[(long long)m * c.dp + slot] = a;
+      continue;
+    }
+    const int bv = (c.s == 2) ? m : (m / g.bh) * c.height + (m % g.bh);
+    for(int t = 0; t < c.s; t++){
+      int v = bv, u = a;
+      if(t > 0){
+        const int deg = (c.s == 2) ? 180 : 90 * t;
+        v = grid_rot(&g, bv, deg);
+        u = grid_rot(&g, a, deg);
+      }
+      c.nbr[(long long)c.itable[v] * c.dp + slot] = c.itable[u];
+    }
+  }
+}
+
 __global__ void anneal_propose_kernel(gbx_chain *chains, int count)
 {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -102,17 +139,24 @@ __global__ void anneal_propose_kernel(gbx_chain *chains, int count)
   dev_rng rng;
   for(int k = 0; k < 31; k++) rng.ring[k] = c.ring[k];
   rng.pos = c.ring_pos;
-  mut_general g = chain_graph(c);
   ODP_Restore r;
   int e = 0;
-  for(int attempt = 0; attempt < ANNEAL_MAX_ATTEMPTS && e == 0; attempt++) e = mut_two_opt(&rng, &g, &r);
+  if(c.grid){
+    mut_grid g = chain_grid(c);
+    for(int attempt = 0; attempt < ANNEAL_MAX_ATTEMPTS && e == 0; attempt++) e = mut_grid_two_opt(&rng, &g, &r);
+    if(e == 1) apply_to_nbr_grid(c, g);
+  }
+  else{
+    mut_general g = chain_graph(c);
+    for(int attempt = 0; attempt < ANNEAL_MAX_ATTEMPTS && e == 0; attempt++) e = mut_two_opt(&rng, &g, &r);
+    if(e == 1) apply_to_nbr(c, g);
+  }
   for(int k = 0; k < 31; k++) c.ring[k] = rng.ring[k];
   c.ring_pos = rng.pos;
   if(e != 1){
     c.status = GBX_CHAIN_ERR_SWAP;
     return;
   }
-  apply_to_nbr(c, g);
   c.last = r;
 }
 
@@ -185,9 +229,16 @@ anneal_decide_kernel(gbx_chain *chains, int count, const gbx_graph_acc *acc, con
   __syncthreads();                       /* the copy has read adj before an undo rewrites it */
   if(threadIdx.x == 0 && sh_run){
     if(!sh_accept){
-      mut_general g = chain_graph(c);
-      mut_restore(&g, &c.last);
-      apply_to_nbr(c, g);
+      if(c.grid){
+        mut_grid g = chain_grid(c);
+        mut_grid_restore(&g, &c.last);
+        apply_to_nbr_grid(c, g);
+      }
+      else{
+        mut_general g = chain_graph(c);
+        mut_restore(&g, &c.last);
+        apply_to_nbr(c, g);
+      }
     }
     c.temp *= c.cooling;
   }

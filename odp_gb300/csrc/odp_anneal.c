@@ -28,13 +28,26 @@ struct odpx_anneal {
   char *d_state_init;
 };
 
+static int chain_nodes(const ODPX_Chain *c)
+{
+  return c->grid ? c->width * c->height : c->nodes;
+}
+
 static int check_chain(const ODPX_Chain *c)
 {
-  if(!c->adjacency || c->nodes <= 0 || c->degree <= 0 || c->symmetries <= 0) return ODPX_ERR_INVALID;
-  if(c->nodes % c->symmetries) return ODPX_ERR_INVALID;
+  if(!c->adjacency || c->degree <= 0 || c->symmetries <= 0) return ODPX_ERR_INVALID;
+  if(c->grid){
+    /* the grid 2-opt takes s = 1, 2 or 4 (utils.c:125-133), 4 on square grids */
+    if(c->width <= 0 || c->height <= 0 || c->length <= 0) return ODPX_ERR_INVALID;
+    if(c->symmetries != 1 && c->symmetries != 2 && c->symmetries != 4) return ODPX_ERR_INVALID;
+    if(c->symmetries > 1 && c->width % 2) return ODPX_ERR_INVALID;
+    if(c->symmetries == 4 && (c->height % 2 || c->width != c->height)) return ODPX_ERR_INVALID;
+  }
+  else if(c->nodes <= 0) return ODPX_ERR_INVALID;
+  if(chain_nodes(c) % c->symmetries) return ODPX_ERR_INVALID;
   if(!c->hill_climbing && (!(c->max_temp > 0) || !(c->min_temp > 0) || c->ncalcs <= 0)) return ODPX_ERR_INVALID;
   if(c->num_degrees){
-    int base = c->nodes / c->symmetries;
+    int base = chain_nodes(c) / c->symmetries;
     for(int i = 0; i < base; i++)
       if(c->num_degrees[i] < 0 || c->num_degrees[i] > c->degree) return ODPX_ERR_INVALID;
   }
@@ -69,7 +82,10 @@ int ODPX_Anneal_create(const ODPX_Chain *chains, int count, ODPX_Anneal **out)
   if(!a || !shapes || !adj || !res){ rc = ODPX_ERR_MEMORY; goto fail; }
   a->count = count;
   for(int i = 0; i < count; i++){
-    shapes[i].nodes = chains[i].nodes;
+    shapes[i].grid = chains[i].grid != 0;
+    shapes[i].nodes = chain_nodes(&chains[i]);
+    shapes[i].width = chains[i].width;
+    shapes[i].height = chains[i].height;
     shapes[i].degree = chains[i].degree;
     shapes[i].symmetries = chains[i].symmetries;
     shapes[i].num_degrees = chains[i].num_degrees;
@@ -103,6 +119,9 @@ int ODPX_Anneal_create(const ODPX_Chain *chains, int count, ODPX_Anneal **out)
     gbx_chain *c = &a->h_chains[i];
     size_t words = (size_t)g->B * g->d;
     c->n = g->n; c->d = g->d; c->dp = g->dp; c->s = g->s; c->base = g->B; c->graph = i;
+    c->grid = in->grid != 0;
+    c->width = in->width; c->height = in->height; c->len = in->length;
+    c->itable = g->has_itable ? p->d_itable + g->itable_off : NULL;
     c->adj = p->d_adj + g->adj_off;
     c->nbr = p->d_nbr + g->nbr_off;
     c->best_adj = a->d_best + boff;

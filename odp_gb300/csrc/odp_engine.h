@@ -149,6 +149,8 @@ int  gbx_event_elapsed_ms(void *start, void *stop, float *ms);
  * of a plan whose tables `adj` and `nbr` point into. */
 typedef struct {
   int n, d, dp, s, base, graph;
+  int grid, width, height, len;  /* grid chains: vertex x*height + y, edges up to len long */
+  const int *itable;           /* grid symmetry: vertex -> neighbour-table row, else NULL */
   int *adj;                    /* compact int[base][d] */
   int *nbr;                    /* neighbour table int[n][dp] */
   const int *ndeg;             /* degree per base row, or NULL (regular) */

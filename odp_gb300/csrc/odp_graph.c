@@ -46,13 +46,7 @@ typedef odp_rng mut_rng;
 
 typedef mut_general gen_ctx;  /* a symmetric general graph: n vertices, s orbits */
 
-typedef struct {              /* a (possibly rotation-symmetric) grid graph */
-  int w, h, d, s, len, n;
-  int bw, bh;                 /* base block: x < bw, y < bh */
-  const int *ndeg;            /* per local row degree, or NULL */
-  int *adj;                   /* int[n/s][d], rows in local-index order */
-  const int *xy;              /* optional (x, y) per vertex: saves divisions */
-} grid_ctx;
+typedef mut_grid grid_ctx;     /* a (possibly rotation-symmetric) grid graph */
 
 static inline int wrap(int x, int n) { return mut_wrap(x, n); }  /* NORM, utils.c:171-177 */
 
@@ -76,87 +70,6 @@ static bool gen_two_opt(odp_rng *rng, gen_ctx *g, ODP_Restore *r)
 /* Grid graphs: vertex v = x*h + y; symmetric grids store the base block.    */
 /* ------------------------------------------------------------------------ */
 
-static inline int gx(int v, int h) { return v / h; }
-static inline int gy(int v, int h) { return v % h; }
-
-/* ODP_ROTATE (utils.c:67-88) for s = 2 (180 degrees) and s = 4 (90/180/270, w == h). */
-static inline int grid_rot(const grid_ctx *g, int v, int deg)
-{
-  int x = gx(v, g->h), y = gy(v, g->h), h = g->h;
-  if(g->s == 2) return (g->w - x - 1) * h + (h - y - 1);
-  if(deg == 90)  return y * h + (h - x - 1);
-  if(deg == 180) return (h - x - 1) * h + (h - y - 1);
-  return (h - y - 1) * h + x;
-}
-
-/* Row of a base-block vertex (ODP_LOCAL_INDEX_GRID, utils.c:189-211). */
-static inline int grid_row(const grid_ctx *g, int v)
-{
-  if(g->s != 4) return v;
-  return gx(v, g->h) * g->bh + gy(v, g->h);
-}
-
-/* adjacency[v][j] of the expanded grid (GLOBAL_ADJ_GRID, utils.c:214-247). */
-static inline int grid_nbr(const grid_ctx *g, int v, int j)
-{
-  const int d = g->d;
-  if(g->s == 1) return g->adj[(size_t)v * d + j];
-  int x = gx(v, g->h), y = gy(v, g->h);
-  if(g->s == 2){
-    if(x < g->bw) return g->adj[(size_t)v * d + j];
-    return grid_rot(g, g->adj[(size_t)grid_rot(g, v, 180) * d + j], 180);
-  }
-  if(x < g->bw && y < g->bh) return g->adj[(size_t)grid_row(g, v) * d + j];
-  if(x < g->bw)  return grid_rot(g, g->adj[(size_t)grid_row(g, grid_rot(g, v, 270)) * d + j], 90);
-  if(y >= g->bh) return grid_rot(g, g->adj[(size_t)grid_row(g, grid_rot(g, v, 180)) * d + j], 180);
-  return grid_rot(g, g->adj[(size_t)grid_row(g, grid_rot(g, v, 90)) * d + j], 270);
-}
-
-/* Base row that stores vertex v's orbit (global2local_vertex_grid, utils.c:392-423). */
-static inline int grid_orbit_row(const grid_ctx *g, int v)
-{
-  if(g->s == 1) return v;
-  int x = gx(v, g->h), y = gy(v, g->h);
-  if(g->s == 2) return (x < g->bw) ? v : grid_rot(g, v, 180);
-  if(x < g->bw && y < g->bh) return grid_row(g, v);
-  if(x < g->bw)  return grid_row(g, grid_rot(g, v, 270));
-  if(y >= g->bh) return grid_row(g, grid_rot(g, v, 180));
-  return grid_row(g, grid_rot(g, v, 90));
-}
-
-/* adjacency[v][slot] = u through the symmetry (set_adjacency, utils.c:425-459). */
-static void grid_put(grid_ctx *g, int v, int slot, int u)
-{
-  const int d = g->d;
-  if(g->s == 1){ g->adj[(size_t)v * d + slot] = u; return; }
-  int x = gx(v, g->h), y = gy(v, g->h);
-  if(g->s == 2){
-    if(x < g->bw) g->adj[(size_t)v * d + slot] = u;
-    else g->adj[(size_t)grid_rot(g, v, 180) * d + slot] = grid_rot(g, u, 180);
-    return;
-  }
-  if(x < g->bw && y < g->bh)
-    g->adj[(size_t)grid_row(g, v) * d + slot] = u;
-  else if(x < g->bw)
-    g->adj[(size_t)grid_row(g, grid_rot(g, v, 270)) * d + slot] = grid_rot(g, u, 270);
-  else if(y >= g->bh)
-    g->adj[(size_t)grid_row(g, grid_rot(g, v, 180)) * d + slot] = grid_rot(g, u, 180);
-  else
-    g->adj[(size_t)grid_row(g, grid_rot(g, v, 90)) * d + slot] = grid_rot(g, u, 90);
-}
-
-static inline int grid_deg(const grid_ctx *g, int v)
-{
-  return g->ndeg ? g->ndeg[grid_orbit_row(g, v)] : g->d;
-}
-
-static inline bool grid_short(const grid_ctx *g, int u, int v)      /* CHECK_LENGTH, utils.c:52-56 */
-{
-  if(g->xy)
-    return abs(g->xy[2 * u] - g->xy[2 * v]) + abs(g->xy[2 * u + 1] - g->xy[2 * v + 1]) <= g->len;
-  return abs(gx(u, g->h) - gx(v, g->h)) + abs(gy(u, g->h) - gy(v, g->h)) <= g->len;
-}
-
 static int *grid_coords(int w, int h)
 {
   int *xy = malloc(sizeof(int) * 2 * (size_t)w * h);
@@ -164,173 +77,13 @@ static int *grid_coords(int w, int h)
   return xy;
 }
 
-static inline bool grid_is_antipodal(const grid_ctx *g, int u, int v)  /* IS_DIAMETER_GRID, utils.c:104-110 */
-{
-  return g->s != 1 && u == grid_rot(g, v, 180);
-}
-
-/* get_degree_index_grid, utils.c:534-557 */
-static int grid_back_slot(const grid_ctx *g, int u, int v, int u_slot)
-{
-  if(u == v){
-    int dd = grid_deg(g, v);
-    for(int i = 0; i < dd; i++)
-      if(grid_nbr(g, v, i) == u && i != u_slot) return i;
-  }
-  else if(g->s != 1 && u == grid_rot(g, v, 180)){
-    return u_slot;
-  }
-  else{
-    int dd = grid_deg(g, v);
-    for(int i = 0; i < dd; i++)
-      if(grid_nbr(g, v, i) == u) return i;
-  }
-  ODP_FAIL("Something Wrong ! [id=5]\n");
-}
-
-/* check_rotated_edges_overlap_grid, utils.c:766-782 */
-static bool grid_same_orbit(const grid_ctx *g, int u0, int v0, int u1, int v1)
-{
-  if(g->s == 2)
-    return (u0 == grid_rot(g, u1, 180) && v0 == grid_rot(g, v1, 180)) ||
-           (u0 == grid_rot(g, v1, 180) && v0 == grid_rot(g, u1, 180));
-  if(g->s == 4){
-    for(int deg = 90; deg <= 270; deg += 90)
-      if(u0 == grid_rot(g, u1, deg) && v0 == grid_rot(g, v1, deg)) return true;
-    for(int deg = 90; deg <= 270; deg += 90)
-      if(u0 == grid_rot(g, v1, deg) && v0 == grid_rot(g, u1, deg)) return true;
-  }
-  return false;
-}
-
-/* mutate_adjacency_1opt_grid_s, utils.c:790-822 */
-static bool grid_one_opt(odp_rng *rng, grid_ctx *g, int u, int us)
-{
-  int s = g->s;
-  int v = grid_nbr(g, u, us);
-  if(grid_is_antipodal(g, u, v)) return false;
-  if(s == 2 && u == grid_rot(g, v, 180)) return false;
-  if(s == 4 && (u == grid_rot(g, v, 90) || u == grid_rot(g, v, 270))) return false;
-  int vs = grid_back_slot(g, u, v, us);
-  int k = odp_rng_below(rng, s);
-  if(k != s - 1){
-    int nv = grid_rot(g, v, (k + 1) * (360 / s));
-    int nu = grid_rot(g, u, (s - k - 1) * (360 / s));
-    if(!grid_short(g, u, nv)) return false;
-    grid_put(g, nv, vs, u);
-    grid_put(g, nu, us, v);
-  }
-  else{
-    int nv = grid_rot(g, u, 180);
-    int nu = grid_rot(g, v, 180);
-    if(!grid_short(g, u, nv) || !grid_short(g, v, nu)) return false;
-    grid_put(g, nv, us, u);
-    grid_put(g, nu, vs, v);
-  }
-  return true;
-}
-
-/* One 2-opt attempt on a grid(_s) graph (mutate_adjacency_2opt_grid_s, utils.c:824-971). */
+/* One 2-opt attempt on a grid(_s) graph; false when the attempt is rejected
+ * and the caller retries. */
 static bool grid_two_opt(odp_rng *rng, grid_ctx *g, ODP_Restore *r)
 {
-  int u[2], v[2], us[2], vs[2];
-  const int n = g->n;
-  for(;;){
-    u[0] = odp_rng_below(rng, n);
-    u[1] = odp_rng_below(rng, n);
-    if(u[0] == u[1]) continue;
-    us[0] = odp_rng_below(rng, grid_deg(g, u[0]));
-    v[0] = grid_nbr(g, u[0], us[0]);
-    if(v[0] == u[1]) continue;
-    us[1] = odp_rng_below(rng, grid_deg(g, u[1]));
-    v[1] = grid_nbr(g, u[1], us[1]);
-    if(v[1] == u[0] || v[0] == v[1]) continue;
-    break;
-  }
-  /* Reverse slots are resolved lazily (see file header): vs_ready tracks it. */
-  bool vs_ready = false;
-#define RESOLVE_BACK_SLOTS() do{ if(!vs_ready){ \
-    vs[0] = grid_back_slot(g, u[0], v[0], us[0]); \
-    vs[1] = grid_back_slot(g, u[1], v[1], us[1]); \
-    fill_restore(r, u, us, v, vs); vs_ready = true; } }while(0)
-
-  bool a0 = grid_is_antipodal(g, u[0], v[0]), a1 = grid_is_antipodal(g, u[1], v[1]);
-  if(a0 && a1){
-    if(g->s == 4 && (u[0] == grid_rot(g, u[1], 90) || u[0] == grid_rot(g, u[1], 270))) return false;
-    int t0, t1;
-    if(odp_rng_below(rng, 2)){ if(!grid_short(g, u[0], u[1])) return false; t0 = u[1]; t1 = u[0]; }
-    else                     { if(!grid_short(g, u[0], v[1])) return false; t0 = v[1]; t1 = v[0]; }
-    RESOLVE_BACK_SLOTS();
-    grid_put(g, u[0], us[0], t0);
-    grid_put(g, u[1], us[1], t1);
-    return true;
-  }
-  if(a0 || a1){
-    RESOLVE_BACK_SLOTS();       /* the restore record keeps the unswapped order */
-    if(a1){
-      int t;
-      t = u[0]; u[0] = u[1]; u[1] = t;
-      t = us[0]; us[0] = us[1]; us[1] = t;
-      t = v[0]; v[0] = v[1]; v[1] = t;
-      t = vs[0]; vs[0] = vs[1]; vs[1] = t;
-    }
-    int k = odp_rng_below(rng, 4), t[4];
-    int u1o = grid_rot(g, u[1], 180), v1o = grid_rot(g, v[1], 180);
-    switch(k){
-    case 0:
-      if(!grid_short(g, u[0], v[1]) || !grid_short(g, u[1], u1o)) return false;
-      t[0] = v[1]; t[1] = u1o; t[2] = v1o; t[3] = u[0];
-      break;
-    case 1:
-      if(!grid_short(g, u[0], v1o) || !grid_short(g, u[1], u1o)) return false;
-      t[0] = v1o; t[1] = u1o; t[2] = v[1]; t[3] = v[0];
-      break;
-    case 2:
-      if(!grid_short(g, u[0], u[1]) || !grid_short(g, v[1], v1o)) return false;
-      t[0] = u[1]; t[1] = u[0]; t[2] = u1o; t[3] = v1o;
-      break;
-    default:
-      if(!grid_short(g, u[0], u1o) || !grid_short(g, v[1], v1o)) return false;
-      t[0] = u1o; t[1] = v[0]; t[2] = u[1]; t[3] = v1o;
-      break;
-    }
-    grid_put(g, u[0], us[0], t[0]);
-    grid_put(g, u[1], us[1], t[1]);
-    grid_put(g, v[0], vs[0], t[2]);
-    grid_put(g, v[1], vs[1], t[3]);
-    return true;
-  }
-
-  if(grid_same_orbit(g, u[0], v[0], u[1], v[1])){
-    RESOLVE_BACK_SLOTS();
-    return grid_one_opt(rng, g, u[0], us[0]);
-  }
-
-  int t[4];
-  int cross = odp_rng_below(rng, 2);
-  {
-    /* Length test first and without a data-dependent branch: almost every
-     * proposal on a large grid fails here. */
-    int pu = cross ? v[1] : u[1], pv = cross ? u[1] : v[1];
-    if(!(grid_short(g, u[0], pu) & grid_short(g, v[0], pv))) return false;
-  }
-  if(cross){                            /* u0--v1, v0--u1 */
-    if(grid_is_antipodal(g, u[0], v[1]) || grid_is_antipodal(g, v[0], u[1])) return false;
-    if(grid_same_orbit(g, u[0], v[1], v[0], u[1])) return false;
-    t[0] = v[1]; t[1] = v[0]; t[2] = u[1]; t[3] = u[0];
-  }
-  else{                                 /* u0--u1, v0--v1 */
-    if(grid_is_antipodal(g, u[0], u[1]) || grid_is_antipodal(g, v[0], v[1])) return false;
-    if(grid_same_orbit(g, u[0], u[1], v[0], v[1])) return false;
-    t[0] = u[1]; t[1] = u[0]; t[2] = v[1]; t[3] = v[0];
-  }
-  RESOLVE_BACK_SLOTS();
-  grid_put(g, u[0], us[0], t[0]);
-  grid_put(g, u[1], us[1], t[1]);
-  grid_put(g, v[0], vs[0], t[2]);
-  grid_put(g, v[1], vs[1], t[3]);
-  return true;
-#undef RESOLVE_BACK_SLOTS
+  int e = mut_grid_two_opt(rng, g, r);
+  if(e < 0) ODP_FAIL("Something Wrong ! [id=5]\n");
+  return e == 1;
 }
 
 /* ------------------------------------------------------------------------ */
@@ -862,6 +615,20 @@ void ODPX_Mutate_adjacency_general_s_rng(void *rng_state, int nodes, int degree,
                                          int symmetries, ODP_Restore *r, int *adjacency)
 {
   odpx_mutate_general((odp_rng *)rng_state, nodes, degree, num_degrees, symmetries, r, adjacency);
+}
+
+/* The grid counterparts (ODP_Mutate_adjacency_grid_s / ODP_Restore_adjacency_grid
+ * with an explicit stream and shape). */
+void ODPX_Mutate_adjacency_grid_s_rng(void *rng_state, int width, int height, int degree, const int *num_degrees,
+                                      int length, int symmetries, ODP_Restore *r, int *adjacency)
+{
+  odpx_mutate_grid((odp_rng *)rng_state, width, height, degree, num_degrees, length, symmetries, r, adjacency);
+}
+
+void ODPX_Restore_adjacency_grid_s(int width, int height, int degree, int symmetries, ODP_Restore r, int *adjacency)
+{
+  check_grid_sym(width, height, symmetries);
+  odpx_restore_grid(width, height, degree, symmetries, r, adjacency);
 }
 
 size_t ODPX_Rng_size(void) { return sizeof(odp_rng); }

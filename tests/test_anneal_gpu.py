@@ -1,6 +1,7 @@
 """Annealing chains on the GPU (ODPX_Anneal_*) against the reference's
-annealing loop restated on the host: sample/SA/general.c:160-191 and
-general_s.c:170-191 (Mutate, Set_aspl, best tracking, accept_s, Restore when
+annealing loop restated on the host: sample/SA/general.c:160-191,
+general_s.c:170-191, grid.c:170-191 and grid_s.c:180-201 (Mutate, Set_aspl,
+best tracking, accept_s, Restore when
 rejected, temp *= cooling_rate) with accept_s and uniform_rand from
 sample/SA/common.c:10-37.  On the host the 2-opt swaps come from the library's
 host utilities on the same private stream (ODP_Srand(seed) equivalent) and the
@@ -33,6 +34,9 @@ class HostChain:
 
     def evaluate(self):
         c = self.c
+        if c.grid:
+            return tuple(oracle.aspl(self.adj, symmetries=c.symmetries, num_degrees=c.num_degrees, grid=True,
+                                     width=c.width, height=c.height))
         return tuple(oracle.aspl(self.adj, nodes=c.nodes, symmetries=c.symmetries, num_degrees=c.num_degrees))
 
     def accept(self, d, a):                     # accept_s, common.c:15-37
@@ -51,8 +55,12 @@ class HostChain:
 
     def step(self):
         c = self.c
-        r = self.rng.mutate_general(c.nodes, c.degree, self.adj, symmetries=c.symmetries,
-                                    num_degrees=c.num_degrees)
+        if c.grid:
+            r = self.rng.mutate_grid(c.width, c.height, c.degree, c.length, self.adj, symmetries=c.symmetries,
+                                     num_degrees=c.num_degrees)
+        else:
+            r = self.rng.mutate_general(c.nodes, c.degree, self.adj, symmetries=c.symmetries,
+                                        num_degrees=c.num_degrees)
         d, s, a = self.evaluate()
         self.steps += 1
         if d < self.best[0] or (d == self.best[0] and a < self.best[2]):
@@ -60,6 +68,8 @@ class HostChain:
         if self.accept(d, a):
             self.cur = (d, s, a)
             self.accepted += 1
+        elif c.grid:
+            og.Rng.restore_grid(c.width, c.height, c.degree, r, self.adj, symmetries=c.symmetries)
         else:
             og.Rng.restore_general(c.nodes, c.degree, r, self.adj, symmetries=c.symmetries)
         self.temp *= self.cooling
@@ -118,6 +128,42 @@ def test_device_chains_follow_the_reference_loop():
                 assert np.array_equal(st["adjacency"], h.adj), k
                 assert np.array_equal(st["best_adjacency"], h.best_adj), k
         assert any(0 < h.accepted < h.steps for h in host)   # both outcomes were exercised
+    finally:
+        dev.close()
+
+
+def grid(w, h, d, length, s=1, seed=1):
+    e = og.generate_random_grid(w, h, d, length, s, seed=seed)
+    return og.conv_edge2adjacency_grid(w, h, e, d, s)
+
+
+def test_device_grid_chains_follow_the_reference_loop():
+    """sample/SA/grid.c:170-191 and grid_s.c:180-201: the grid 2-opt with its
+    length limit, for s = 1, 2 and 4."""
+    cs = [og.Chain(grid(12, 12, 4, 3, seed=41), grid=True, width=12, height=12, length=3, seed=51, max_temp=20.0,
+                   min_temp=0.2, ncalcs=60),
+          og.Chain(grid(12, 10, 4, 4, 2, seed=42), grid=True, width=12, height=10, length=4, symmetries=2, seed=52,
+                   max_temp=20.0, min_temp=0.2, ncalcs=60),
+          og.Chain(grid(12, 12, 6, 3, 4, seed=43), grid=True, width=12, height=12, length=3, symmetries=4, seed=53,
+                   max_temp=20.0, min_temp=0.2, ncalcs=60),
+          og.Chain(grid(10, 10, 4, 5, seed=44), grid=True, width=10, height=10, length=5, seed=54, hill_climbing=True)]
+    host = [HostChain(c) for c in cs]
+    dev = og.Anneal(cs)
+    try:
+        for run in (9, 21):
+            dev.run(run)
+            for h in host:
+                for _ in range(run):
+                    h.step()
+            for k, h in enumerate(host):
+                st = dev.state(k, graphs=True)
+                assert st["status"] == 0, (k, st["status"])
+                assert st["steps"] == h.steps and st["accepted"] == h.accepted, (k, st, h.accepted)
+                assert same((st["diameter"], st["sum"], st["aspl"]), h.cur), k
+                assert same((st["best_diameter"], st["best_sum"], st["best_aspl"]), h.best), k
+                assert np.array_equal(st["adjacency"], h.adj), k
+                assert np.array_equal(st["best_adjacency"], h.best_adj), k
+        assert any(0 < h.accepted < h.steps for h in host)
     finally:
         dev.close()
 
