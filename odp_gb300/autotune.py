@@ -65,11 +65,12 @@ def measure(specs, repeats=3, flush_mb=256):
         b.close()
 
 
-def tune_batch(specs, slots=(32, 64, 128), local_kb=(256, 2048), widths=(3, 4, 5, 6, 7), repeats=3,
-               max_buckets=12):
+def tune_batch(specs, slots=(32, 64, 128), local_kb=(256, 2048), widths=(3, 4, 5, 6, 7), tile_kb=(128, 640, 1280),
+               repeats=3, max_buckets=12):
     """Tunes a batch: a global pass over slots and the local-job threshold,
-    then a per-bucket pass over chunk widths (buckets in order of their share
-    of the work).  Installs and returns the result."""
+    then a per-bucket pass over chunk widths and, for the chosen width, tile
+    traffic (buckets in order of their share of the work).  Installs and
+    returns the result."""
     t0 = time.perf_counter()
     clear()
     base = measure(specs, repeats)
@@ -96,12 +97,19 @@ def tune_batch(specs, slots=(32, 64, 128), local_kb=(256, 2048), widths=(3, 4, 5
             set_table(trial)
             ms = measure(specs, repeats)
             if ms < current:
-                current, choice = ms, wl
+                current, choice = ms, {"wc_log2": wl}
         if choice is not None:
-            table[bk] = {"wc_log2": choice}
+            table[bk] = choice
+        for tk in tile_kb:
+            trial = dict(table)
+            trial[bk] = dict(table.get(bk, {}), tile_kb=tk)
+            set_table(trial)
+            ms = measure(specs, repeats)
+            if ms < current:
+                current, table[bk] = ms, trial[bk]
         set_table(table)
     return {"default_ms": base, "tuned_ms": current, "slots": best[1], "local_kb": best[2],
-            "buckets": {"%d/%d/%d" % k: v["wc_log2"] for k, v in table.items()},
+            "buckets": {"%d/%d/%d" % k: v for k, v in table.items()},
             "seconds": time.perf_counter() - t0}
 
 
