@@ -198,14 +198,25 @@ def run_reference(args):
     if rank != 0:
         return
     shapes, specs = batch_workload(args.graphs)
-    steps = max(1, min(args.steps, 3))
-    v, done, dt, _, cores = oracle_sample(specs, args.cpu_seconds)
-    line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 / v, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "u64", "data": "synthetic (reference generators, seeded)",
+    # every step is a bounded sample of the batch (its first graphs, in order,
+    # for a fixed slice of CPU time), so the whole run stays near two minutes
+    per_step = min(2.0, 120.0 / max(1, args.steps + args.warmup))
+    for _ in range(args.warmup):
+        oracle_sample(specs, per_step)
+    total_done, total_s, cores = 0, 0.0, 1
+    for _ in range(args.steps):
+        _, done, dt, _, cores = oracle_sample(specs, per_step)
+        total_done += done
+        total_s += dt
+    v = total_done / total_s
+    line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (reference generators, seeded)",
             "impl": "reference", "config": {"workload": WORKLOAD, "graphs": len(specs)},
             "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
-                             "sample": "first %d graphs of the batch, %.1f s" % (done, dt)},
+                             "sample": "per step, the batch's first graphs for %.2f s of CPU time (%d graphs "
+                                       "over %d steps)" % (per_step, total_done, args.steps)},
             "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
