@@ -84,8 +84,9 @@ double ODPX_Batch_bytes_alg(const ODPX_Batch *batch);
  * buffer of `megabytes`, `reps` times: the L2 ceiling of the roofline. */
 double ODPX_Measure_l2_read_gbs(int megabytes, int reps);
 
-/* Tuning knobs for plans created after the call (0 = automatic; use_graph:
- * -1 automatic, 0 off, 1 on). */
+/* Tuning knobs for plans created after the call, batch plans and the
+ * drop-in ODP_Init_aspl_* alike (0 = automatic; use_graph: -1 automatic,
+ * 0 off, 1 on). */
 void ODPX_Set_tuning(int wc_log2, int slots, int tile_rows, int l2_budget_mb, int local_kb, int use_graph);
 
 /* Per-bucket tuning table consulted when plans are created (the autotuner

@@ -111,7 +111,7 @@ static void init_common(const odp_shape *sh)
   S.symmetries = sh->symmetries;
   S.profile = profile_requested();
   odp_tuning t;
-  odp_tuning_defaults(&t, 0);
+  odp_tuning_for(1, &t);
   int rc = odp_plan_create(sh, 1, &t, &S.plan);
   if(rc == ODPX_ERR_INVALID) fail("Invalid graph parameters (nodes=%d, symmetries=%d)\n", nodes, sh->symmetries);
   if(rc) fail("GPU initialisation failed (error %d)\n", rc);

@@ -25,7 +25,9 @@ void ODPX_Set_tuning(int wc_log2, int slots, int tile_rows, int l2_budget_mb, in
   g_override_set = 1;
 }
 
-static void tuning_for(int count, odp_tuning *t)
+/* Plan tuning for `count` graphs: the defaults, then the ODPX_Set_tuning
+ * overrides.  The drop-in ODP_Init_aspl_* plans use it too. */
+void odp_tuning_for(int count, odp_tuning *t)
 {
   odp_tuning_defaults(t, count > 1);
   if(!g_override_set) return;
@@ -57,7 +59,7 @@ int ODPX_Batch_create(int count, const ODP_Graph *graphs, ODPX_Batch **batch)
   odp_shape *sh = malloc(sizeof(odp_shape) * (size_t)count);
   for(int i = 0; i < count; i++) to_shape(&graphs[i], &sh[i]);
   odp_tuning t;
-  tuning_for(count, &t);
+  odp_tuning_for(count, &t);
   int rc = odp_plan_create(sh, count, &t, batch);
   free(sh);
   return rc;

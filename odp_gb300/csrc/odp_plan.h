@@ -80,6 +80,8 @@ typedef struct {
 } odp_result;
 
 void odp_tuning_defaults(odp_tuning *t, int batch);
+/* The defaults for `count` graphs with the ODPX_Set_tuning overrides applied. */
+void odp_tuning_for(int count, odp_tuning *t);
 /* Returns 0 on success, else an ODPX_ERR_* code (include/odp_gb300.h). */
 int  odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning, odp_plan **out);
 void odp_plan_destroy(odp_plan *p);
