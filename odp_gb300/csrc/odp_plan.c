@@ -274,16 +274,11 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     int wl;
     if(tuning->wc_log2 > 0) wl = tuning->wc_log2;
     else if(te && te->wc_log2 > 0) wl = te->wc_log2;
-    else if(count > 1){
-      /* batch: 256-byte rows, 64 concurrent jobs (measured best on GB300 for
-       * the 512-graph workload) */
-      wl = full_l2 < 5 ? full_l2 : 5;
-    }
     else{
-      /* 128-byte rows (16 words): measured on GB300 to beat wider rows at
-       * equal L2 footprint, because more chunks can be in flight (several
-       * slots) and their level boundaries overlap */
-      wl = full_l2 < 4 ? full_l2 : 4;
+      /* 256-byte rows (32 words): measured best on GB300 for the 512-graph
+       * batch and for single graphs (n = 1024, 65536, the 262144-vertex s = 64
+       * graph and the 256 x 256 grid) */
+      wl = full_l2 < 5 ? full_l2 : 5;
     }
     if(wl < 1) wl = 1;
     if(wl > 7) wl = 7;                 /* rows of at most 1 KB per chunk */
@@ -295,7 +290,19 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     int rpp = rows_per_pass(wl);
     double local_here = (te && te->local_kb > 0 && tuning->local_kb_explicit == 0) ? te->local_kb * 1024.0
                                                                                    : local_bytes;
-    double tile_bytes = (te && te->tile_kb > 0) ? te->tile_kb * 1024.0 : 288.0 * 1024.0;
+    /* about 640 KB of traffic per tile, measured best on GB300 for large
+     * single graphs and for most size buckets of the batch; a small single
+     * graph takes smaller tiles, enough for about two per CTA over its
+     * concurrently active chunks */
+    double tile_bytes = 640.0 * 1024.0;
+    if(te && te->tile_kb > 0) tile_bytes = te->tile_kb * 1024.0;
+    else if(count == 1){
+      int conc = sh->grid ? 8 : 4;
+      if(g->nchunks < conc) conc = g->nchunks;
+      int blocks = tuning->blocks > 0 ? tuning->blocks : gbx_engine_blocks(0);
+      double fill = level_bytes * conc / (2.0 * (blocks > 0 ? blocks : 1));
+      if(fill < tile_bytes) tile_bytes = fill < 32.0 * 1024.0 ? 32.0 * 1024.0 : fill;
+    }
     if(tuning->tile_rows > 0) g->tile_rows = tuning->tile_rows;
     else if(level_bytes <= local_here) g->tile_rows = g->n;
     else{
@@ -354,8 +361,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   free(jobs);
   free(ord);
 
-  /* Slots: as many concurrent jobs as the L2 budget holds (at least 2 when
-   * there are 2 jobs), capped by the job count. */
+  /* Slots: for batches, as many concurrent jobs as the L2 budget holds, at
+   * least 64; for a single graph a fixed count measured best on GB300 (4 for
+   * general graphs; 8 for grids, whose many short levels leave hand-offs to
+   * hide).  Capped by the job count. */
   size_t max_words = 0, max_rows = 0;
   double sum_fp = 0;
   int fit = 0;
@@ -369,10 +378,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   int nslots = tuning->slots > 0 ? tuning->slots : fit;
   if(tuning->slots <= 0){
     if(nslots < 2) nslots = 2;
-    /* a single grid graph runs many levels with little work each: more
-     * chunks in flight hide the per-level hand-offs */
-    if(count == 1 && shapes[0].grid) nslots = 32;
-    else if(count == 1 && nslots > 4) nslots = 4;
+    if(count == 1) nslots = shapes[0].grid ? 8 : 4;
     if(count > 1 && nslots < 64) nslots = 64;
     if(nslots > 512) nslots = 512;
   }
