@@ -286,33 +286,6 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     g->wc_log2 = wl;
     const int wc = 1 << wl;
     g->nchunks = (g->W + wc - 1) / wc;
-    double level_bytes = (double)g->n * wc * 8.0 * (g->d + 2);
-    int rpp = rows_per_pass(wl);
-    double local_here = (te && te->local_kb > 0 && tuning->local_kb_explicit == 0) ? te->local_kb * 1024.0
-                                                                                   : local_bytes;
-    /* about 640 KB of traffic per tile, measured best on GB300 for large
-     * single graphs and for most size buckets of the batch; a small single
-     * graph takes smaller tiles, enough for about two per CTA over its
-     * concurrently active chunks */
-    double tile_bytes = 640.0 * 1024.0;
-    if(te && te->tile_kb > 0) tile_bytes = te->tile_kb * 1024.0;
-    else if(count == 1){
-      int conc = sh->grid ? 8 : 4;
-      if(g->nchunks < conc) conc = g->nchunks;
-      int blocks = tuning->blocks > 0 ? tuning->blocks : gbx_engine_blocks(0);
-      double fill = level_bytes * conc / (2.0 * (blocks > 0 ? blocks : 1));
-      if(fill < tile_bytes) tile_bytes = fill < 32.0 * 1024.0 ? 32.0 * 1024.0 : fill;
-    }
-    if(tuning->tile_rows > 0) g->tile_rows = tuning->tile_rows;
-    else if(level_bytes <= local_here) g->tile_rows = g->n;
-    else{
-      double per_row = (double)wc * 8.0 * (g->d + 2);
-      int tr = (int)(tile_bytes / per_row);
-      g->tile_rows = ALIGN_UP(tr < rpp ? rpp : tr, rpp);
-    }
-    if(g->tile_rows > g->n) g->tile_rows = g->n;
-    if(g->tile_rows < 1) g->tile_rows = 1;
-    g->ntiles = (g->n + g->tile_rows - 1) / g->tile_rows;
     g->has_ndeg = sh->num_degrees != NULL;
     g->has_itable = g->grid_s;
     g->has_srcpos = sh->grid;             /* grids: spatially compact source chunks */
@@ -326,6 +299,52 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     njobs += g->nchunks;
   }
   p->njobs = njobs;
+
+  /* Tiles: about 640 KB of traffic each, measured best on GB300 for large
+   * single graphs and for most size buckets of the batch.  A plan with few
+   * jobs for the grid (a single graph, a group of annealing chains) takes
+   * smaller tiles, and splits jobs it would otherwise run in one CTA, so
+   * that its concurrently active jobs give every CTA about two tiles per
+   * level. */
+  const int grid_blocks = tuning->blocks > 0 ? tuning->blocks : gbx_engine_blocks(0);
+  double fill_tile = 0;
+  if(njobs * 4 <= grid_blocks){
+    double active = 0;
+    for(int i = 0; i < count; i++){
+      const odp_plan_graph *g = &p->g[i];
+      double lb = (double)g->n * (1 << g->wc_log2) * 8.0 * (g->d + 2);
+      int conc = g->nchunks;
+      if(count == 1){ int cap = shapes[0].grid ? 8 : 4; if(conc > cap) conc = cap; }
+      active += lb * conc;
+    }
+    fill_tile = active / (2.0 * (grid_blocks > 0 ? grid_blocks : 1));
+    if(fill_tile < 32.0 * 1024.0) fill_tile = 32.0 * 1024.0;
+  }
+  for(int i = 0; i < count; i++){
+    odp_plan_graph *g = &p->g[i];
+    const ODPX_Tune_entry *te = table_lookup(g->n, g->d, g->grid);
+    const int wc = 1 << g->wc_log2;
+    double level_bytes = (double)g->n * wc * 8.0 * (g->d + 2);
+    int rpp = rows_per_pass(g->wc_log2);
+    double local_here = (te && te->local_kb > 0 && tuning->local_kb_explicit == 0) ? te->local_kb * 1024.0
+                                                                                   : local_bytes;
+    double tile_bytes = 640.0 * 1024.0;
+    if(te && te->tile_kb > 0) tile_bytes = te->tile_kb * 1024.0;
+    else if(fill_tile > 0 && fill_tile < tile_bytes){
+      tile_bytes = fill_tile;
+      if(!tuning->local_kb_explicit && fill_tile < local_here) local_here = fill_tile;
+    }
+    if(tuning->tile_rows > 0) g->tile_rows = tuning->tile_rows;
+    else if(level_bytes <= local_here) g->tile_rows = g->n;
+    else{
+      double per_row = (double)wc * 8.0 * (g->d + 2);
+      int tr = (int)(tile_bytes / per_row);
+      g->tile_rows = ALIGN_UP(tr < rpp ? rpp : tr, rpp);
+    }
+    if(g->tile_rows > g->n) g->tile_rows = g->n;
+    if(g->tile_rows < 1) g->tile_rows = 1;
+    g->ntiles = (g->n + g->tile_rows - 1) / g->tile_rows;
+  }
 
   /* Jobs, largest first so the long ones start early. */
   gbx_job *jobs = calloc((size_t)njobs, sizeof(gbx_job));
