@@ -24,6 +24,8 @@ Reported on rank 0 as one JSON line:
                loop, one request outstanding per chain, exponential think time
                for a 20k req/s offered cap; evals/s and p50/p99 latency, beside
                the same proposals evaluated one call at a time
+  anneal       the same 64 chains with every step (2-opt proposal, evaluation,
+               acceptance, undo) on the GPU (ODPX_Anneal), in 4 size groups
   cpu_baseline the oracle port of the reference CPU library (OpenMP, all host
                cores) on a bounded sample of the batch
 
