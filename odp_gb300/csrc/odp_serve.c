@@ -422,9 +422,16 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
   g.nchunks = (g.W + wc - 1) / wc;
   double level_bytes = (double)n * wc * 8.0 * (g.d + 2);
   int vpr = wc / 2, lanes_per_row = vpr < 32 ? vpr : 32, rpp = 8 * (32 / lanes_per_row);
-  if(level_bytes <= 2048.0 * 1024.0) g.tile_rows = n;
+  /* Tiles of about 640 KB; a smaller graph takes tiles small enough for
+   * about two per CTA of its lane when it runs alone, so that a request does
+   * not wait on one CTA while the rest of the lane idles. */
+  int lane_blocks = s->lanes[0].blocks > 0 ? s->lanes[0].blocks : 1;
+  double tile_bytes = level_bytes * g.nchunks / (2.0 * lane_blocks);
+  if(tile_bytes > 640.0 * 1024.0) tile_bytes = 640.0 * 1024.0;
+  if(tile_bytes < 32.0 * 1024.0) tile_bytes = 32.0 * 1024.0;
+  if(level_bytes <= tile_bytes) g.tile_rows = n;
   else{
-    int tr = (int)(288.0 * 1024.0 / ((double)wc * 8.0 * (g.d + 2)));
+    int tr = (int)(tile_bytes / ((double)wc * 8.0 * (g.d + 2)));
     if(tr < rpp) tr = rpp;
     g.tile_rows = ALIGN_UP(tr, rpp);
     if(g.tile_rows > n) g.tile_rows = n;
