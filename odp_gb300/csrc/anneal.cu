@@ -25,6 +25,7 @@
  */
 #include <cuda_runtime.h>
 #include <climits>
+#include <cstdint>
 #include <cfloat>
 #include "odp_engine.h"
 
@@ -223,8 +224,21 @@ anneal_decide_kernel(gbx_chain *chains, int count, const gbx_graph_acc *acc, con
   }
   __syncthreads();
   if(sh_copy){
+    /* the pointers are read once: a store through best_adj could otherwise
+     * alias the chain record and force a reload per element */
+    const int *__restrict__ src = c.adj;
+    int *__restrict__ dst = c.best_adj;
     const long long words = (long long)c.base * c.d;
-    for(long long k = threadIdx.x; k < words; k += blockDim.x) c.best_adj[k] = c.adj[k];
+    if(((reinterpret_cast<uintptr_t>(src) | reinterpret_cast<uintptr_t>(dst)) & 15) == 0){
+      const long long q = words >> 2;
+      const int4 *s4 = reinterpret_cast<const int4 *>(src);
+      int4 *d4 = reinterpret_cast<int4 *>(dst);
+      for(long long k = threadIdx.x; k < q; k += blockDim.x) d4[k] = s4[k];
+      for(long long k = (q << 2) + threadIdx.x; k < words; k += blockDim.x) dst[k] = src[k];
+    }
+    else{
+      for(long long k = threadIdx.x; k < words; k += blockDim.x) dst[k] = src[k];
+    }
   }
   __syncthreads();                       /* the copy has read adj before an undo rewrites it */
   if(threadIdx.x == 0 && sh_run){

@@ -102,7 +102,7 @@ int ODPX_Anneal_create(const ODPX_Chain *chains, int count, ODPX_Anneal **out)
 
   size_t best_ints = 0, deg_ints = 0;
   for(int i = 0; i < count; i++){
-    best_ints += (size_t)p->g[i].B * p->g[i].d;
+    best_ints += ((size_t)p->g[i].B * p->g[i].d + 3) & ~(size_t)3;   /* 16-byte aligned copies */
     if(chains[i].num_degrees) deg_ints += (size_t)p->g[i].B;
   }
   CK(gbx_malloc((void **)&a->d_best, sizeof(int) * (best_ints ? best_ints : 1)));
@@ -126,7 +126,7 @@ int ODPX_Anneal_create(const ODPX_Chain *chains, int count, ODPX_Anneal **out)
     c->nbr = p->d_nbr + g->nbr_off;
     c->best_adj = a->d_best + boff;
     CK(gbx_memcpy_h2d(c->best_adj, in->adjacency, sizeof(int) * words, p->stream));
-    boff += words;
+    boff += (words + 3) & ~(size_t)3;
     if(in->num_degrees){
       CK(gbx_memcpy_h2d(a->d_rowdeg + doff, in->num_degrees, sizeof(int) * (size_t)g->B, p->stream));
       c->ndeg = a->d_rowdeg + doff;
