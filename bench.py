@@ -54,7 +54,7 @@ WORKLOAD = ("batched: 512 graphs, seeds 100..611, n log-uniform [256, 8192], d i
 # DRAM traffic of one engine_kernel launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture,
 # profiles/engine_kernel_batch.md) on the first 128 graphs of the batch, with that launch's algorithmic
 # bytes.  A full batch launch's traffic is taken as this scaled by algorithmic bytes.
-NCU_DRAM = {"bytes": 827731456.0 + 900297728.0, "bytes_alg": 24803482864.0, "graphs": 128}
+NCU_DRAM = {"bytes": 992011264.0 + 934300160.0, "bytes_alg": 24803482864.0, "graphs": 128}
 
 
 def parse():
