@@ -329,8 +329,8 @@ def anneal(seconds, temperature=50.0):
 
     def work(k):
         while time.perf_counter() < stop:
-            groups[k].run(4)
-            counts[k] += 4 * len(idx[k])
+            groups[k].run(8)
+            counts[k] += 8 * len(idx[k])
 
     threads = [threading.Thread(target=work, args=(k,)) for k in range(len(groups))]
     t0 = time.perf_counter()

@@ -20,12 +20,15 @@
 #include "odp_rng.h"
 #include "odp_gb300.h"
 
+#define ANNEAL_GRAPH_STEPS 8   /* steps per replayed CUDA graph */
+
 struct odpx_anneal {
   odp_plan *p;
   int count;
   gbx_chain *h_chains, *d_chains;
   int *d_best, *d_rowdeg;
   char *d_state_init;
+  void *steps_exec;            /* ANNEAL_GRAPH_STEPS steps captured as one CUDA graph */
 };
 
 static int chain_nodes(const ODPX_Chain *c)
@@ -57,6 +60,7 @@ static int check_chain(const ODPX_Chain *c)
 void ODPX_Anneal_destroy(ODPX_Anneal *a)
 {
   if(!a) return;
+  if(a->steps_exec) gbx_graph_destroy(a->steps_exec);
   if(a->p) odp_plan_destroy(a->p);
   gbx_free(a->d_chains); gbx_free(a->d_best); gbx_free(a->d_rowdeg); gbx_free(a->d_state_init);
   free(a->h_chains);
@@ -157,19 +161,42 @@ fail:
   return rc;
 }
 
-int ODPX_Anneal_run(ODPX_Anneal *a, int steps)
+/* One step in stream order: propose, reset the engine state, evaluate, decide. */
+static int enqueue_step(ODPX_Anneal *a)
 {
-  if(!a || steps < 0) return ODPX_ERR_INVALID;
   odp_plan *p = a->p;
   gbx_ctrl *ctrl = (gbx_ctrl *)(p->d_state + p->out_off);
   const unsigned int *err = (const unsigned int *)(p->d_state + p->out_off + sizeof(gbx_ctrl));
   const gbx_graph_acc *acc = (const gbx_graph_acc *)(p->d_state + p->acc_off);
-  for(int s = 0; s < steps; s++){
-    if(gbx_anneal_propose(a->d_chains, a->count, p->stream)) return ODPX_ERR_CUDA;
-    if(gbx_memcpy_d2d(p->d_state, a->d_state_init, p->state_bytes, p->stream)) return ODPX_ERR_CUDA;
-    if(odp_plan_enqueue_engine(p)) return ODPX_ERR_CUDA;
-    if(gbx_anneal_decide(a->d_chains, a->count, acc, ctrl, err, p->stream)) return ODPX_ERR_CUDA;
+  if(gbx_anneal_propose(a->d_chains, a->count, p->stream)) return ODPX_ERR_CUDA;
+  if(gbx_memcpy_d2d(p->d_state, a->d_state_init, p->state_bytes, p->stream)) return ODPX_ERR_CUDA;
+  if(odp_plan_enqueue_engine(p)) return ODPX_ERR_CUDA;
+  if(gbx_anneal_decide(a->d_chains, a->count, acc, ctrl, err, p->stream)) return ODPX_ERR_CUDA;
+  return 0;
+}
+
+int ODPX_Anneal_run(ODPX_Anneal *a, int steps)
+{
+  if(!a || steps < 0) return ODPX_ERR_INVALID;
+  odp_plan *p = a->p;
+  int s = 0;
+  if(steps >= ANNEAL_GRAPH_STEPS){
+    /* full groups of steps replay one captured graph: a launch per group
+     * instead of four operations per step */
+    if(!a->steps_exec){
+      if(gbx_capture_begin(p->stream)) return ODPX_ERR_CUDA;
+      int e = 0;
+      for(int k = 0; k < ANNEAL_GRAPH_STEPS && !e; k++) e = enqueue_step(a);
+      void *ge = NULL;
+      int e2 = gbx_capture_end(p->stream, &ge);
+      if(e || e2) return ODPX_ERR_CUDA;
+      a->steps_exec = ge;
+    }
+    for(; s + ANNEAL_GRAPH_STEPS <= steps; s += ANNEAL_GRAPH_STEPS)
+      if(gbx_graph_launch(a->steps_exec, p->stream)) return ODPX_ERR_CUDA;
   }
+  for(; s < steps; s++)
+    if(enqueue_step(a)) return ODPX_ERR_CUDA;
   return gbx_stream_sync(p->stream) ? ODPX_ERR_CUDA : 0;
 }
 
