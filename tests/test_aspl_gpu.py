@@ -209,6 +209,25 @@ def test_relabelling_invariance_full_size():
     assert base[0] < 10 and base[1] > 0
 
 
+def test_symmetric_equals_expanded_at_large_size():
+    """Size-independent property: a graph with 32-fold circulant symmetry
+    (n = 131072) gives the same results through the symmetric path (4096
+    source rows, rotated neighbour tables) as its full adjacency through the
+    plain path (131072 source rows), and so does a symmetric grid against
+    its expanded form."""
+    n, d, s = 131072, 12, 32
+    e = og.generate_random_general(n, d, s, seed=6)
+    sym = gpu_aspl(og.conv_edge2adjacency_general(n, e, d, s), nodes=n, symmetries=s)
+    full = gpu_aspl(og.conv_edge2adjacency_general(n, e, d, 1), nodes=n)
+    assert same(sym, full)
+    assert sym[0] < 20 and sym[1] > 0
+    w = 128
+    e = og.generate_random_grid(w, w, 6, 5, 4, seed=7)
+    sym = gpu_aspl(og.conv_edge2adjacency_grid(w, w, e, 6, 4), grid=True, width=w, height=w, symmetries=4)
+    full = gpu_aspl(og.conv_edge2adjacency_grid(w, w, e, 6, 1), grid=True, width=w, height=w)
+    assert same(sym, full)
+
+
 def test_out_of_range_adjacency_is_reported():
     n, d = 64, 3
     adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=3), d)
