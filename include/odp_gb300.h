@@ -48,13 +48,18 @@ typedef struct {
 /* Evaluates `count` graphs; results written per graph.  Returns ODPX_*. */
 int ODP_Set_aspl_batch(int count, const ODP_Graph *graphs, int *diameter, long *sum, double *ASPL);
 
-/* Reusable batch plan (same shapes every run). */
+/* Reusable batch plan (same shapes every run).  ODPX_Batch_run evaluates
+ * adjacency[i] (int[n_i/s_i][d_i] each) for graph i and returns when the
+ * results are written; the arrays are read during the call only. */
 typedef struct odp_plan ODPX_Batch;
 int  ODPX_Batch_create(int count, const ODP_Graph *graphs, ODPX_Batch **batch);
 int  ODPX_Batch_run(ODPX_Batch *batch, const int *const *adjacency, int *diameter, long *sum, double *ASPL);
 void ODPX_Batch_destroy(ODPX_Batch *batch);
-/* Device time of the last run's GPU work in ms (CUDA events on the plan's
- * stream), and the tiles the engine processed. */
+/* Device time of the plan's GPU work in ms per run (CUDA events on the
+ * plan's stream).  A non-NULL adjacency is handed over first; with NULL the
+ * arrays of the previous run or timing call are read again, so they must
+ * still be valid and unchanged (on devices that read host memory directly
+ * the plan keeps only their addresses). */
 int  ODPX_Batch_time(ODPX_Batch *batch, const int *const *adjacency, int repeats, float *ms_per_run);
 /* mode 0: whole per-call sequence (upload, expand, engine, read back);
  * mode 1: engine on resident inputs.  flush_mb > 0 overwrites a buffer of
