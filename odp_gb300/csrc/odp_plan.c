@@ -51,7 +51,7 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->local_kb = env_int("ODP_GB300_LOCAL_KB", batch ? 2048 : 96);
   t->use_graph = env_int("ODP_GB300_GRAPH", 1);
   t->blocks = env_int("ODP_GB300_BLOCKS", 0);
-  t->activity = env_int("ODP_GB300_ACTIVITY", 0);
+  t->activity = env_int("ODP_GB300_ACTIVITY", -2);
   t->local_kb_explicit = getenv("ODP_GB300_LOCAL_KB") != NULL;
   t->reorder = env_int("ODP_GB300_REORDER", 1);
   t->direct = env_int("ODP_GB300_DIRECT", 1);
@@ -362,9 +362,15 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
         j->sym = g->s; j->graph = i;
         j->tile_rows = g->tile_rows; j->ntiles = g->ntiles;
         /* Change tracking (gather only words that changed at the previous
-         * level) is exact for every graph; on GB300 its per-row staging costs
-         * about what it saves at these degrees, so it is off unless asked. */
-        int act = tuning->activity < 0 ? g->grid : tuning->activity;
+         * level) is exact for every graph.  On GB300 its per-row staging,
+         * and in a batch the larger staging area of every job, cost more than
+         * it saves, except on large grids evaluated alone: measured -17 % on
+         * the 256 x 256 grid (diameter 140), +5 % to +21 % on single grids of
+         * 64 x 64 to 180 x 180 and +8 % on the 512-graph batch.  So by default
+         * it is on only for a single grid of at least 49152 vertices. */
+        int act;
+        if(tuning->activity == -2) act = count == 1 && g->grid && g->n >= 49152;
+        else act = tuning->activity == -1 ? g->grid : tuning->activity;
         j->flags = act ? GBX_JOB_ACTIVE : 0;
         ord[k].job = k;
         ord[k].work = (double)g->n * wc * (g->d + 2) * (count > 1 ? 1.0 : 0.0);

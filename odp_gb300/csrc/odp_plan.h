@@ -28,7 +28,7 @@ typedef struct {
   int local_kb;                /* per-level traffic at or below which a job runs in one CTA */
   int use_graph;               /* replay through a CUDA graph */
   int blocks;                  /* persistent grid size; 0 = SMs x occupancy */
-  int activity;                /* change tracking: 0 never (default), 1 always, -1 grids only */
+  int activity;                /* change tracking: -2 automatic (default), 0 never, 1 always, -1 grids only */
   int local_kb_explicit;       /* local_kb was set by the caller: the tuning table does not override it */
   int reorder;                 /* after the first run, order jobs by their measured duration (1, default) */
   int direct;                  /* pull callers' adjacency from host memory when the device can (1, default) */
