@@ -232,6 +232,19 @@ static void fill_state_init(odp_plan *p)
   ctrl->next_job = (unsigned)p->nslots;
 }
 
+/* Whether a graph's jobs track changes (gather only words that changed at
+ * the previous level).  It is exact for every graph.  On GB300 its per-row
+ * staging, and in a batch the larger staging area of every job, cost more
+ * than it saves, except on large grids evaluated alone: measured -17 % on the
+ * 256 x 256 grid (diameter 140), +5 % to +21 % on single grids of 64 x 64 to
+ * 180 x 180 and +8 % on the 512-graph batch.  So by default it is on only
+ * for a single grid of at least 49152 vertices. */
+static int tracks_changes(const odp_tuning *t, int count, int grid, int n)
+{
+  if(t->activity == -2) return count == 1 && grid && n >= 49152;
+  return t->activity == -1 ? grid : t->activity;
+}
+
 #define CK(call) do{ int _e = (call); if(_e){ rc = ODPX_ERR_CUDA; goto fail; } }while(0)
 
 int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning, odp_plan **out)
@@ -274,10 +287,15 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     int wl;
     if(tuning->wc_log2 > 0) wl = tuning->wc_log2;
     else if(te && te->wc_log2 > 0) wl = te->wc_log2;
+    else if(tracks_changes(tuning, count, sh->grid, g->n)){
+      /* 512-byte rows for a grid with change tracking (the 256 x 256 grid:
+       * 24.4 ms with 64 words and 16 slots against 28.8 ms with 32 and 8) */
+      wl = full_l2 < 6 ? full_l2 : 6;
+    }
     else{
       /* 256-byte rows (32 words): measured best on GB300 for the 512-graph
        * batch and for single graphs (n = 1024, 65536, the 262144-vertex s = 64
-       * graph and the 256 x 256 grid) */
+       * graph and grids without change tracking) */
       wl = full_l2 < 5 ? full_l2 : 5;
     }
     if(wl < 1) wl = 1;
@@ -314,7 +332,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       const odp_plan_graph *g = &p->g[i];
       double lb = (double)g->n * (1 << g->wc_log2) * 8.0 * (g->d + 2);
       int conc = g->nchunks;
-      if(count == 1){ int cap = shapes[0].grid ? 8 : 4; if(conc > cap) conc = cap; }
+      if(count == 1){
+        int cap = !g->grid ? 4 : tracks_changes(tuning, 1, 1, g->n) ? 16 : 8;
+        if(conc > cap) conc = cap;
+      }
       active += lb * conc;
     }
     fill_tile = active / (2.0 * (grid_blocks > 0 ? grid_blocks : 1));
@@ -361,17 +382,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
         j->nsrc = g->B - j->src0 < wc * 64 ? g->B - j->src0 : wc * 64;
         j->sym = g->s; j->graph = i;
         j->tile_rows = g->tile_rows; j->ntiles = g->ntiles;
-        /* Change tracking (gather only words that changed at the previous
-         * level) is exact for every graph.  On GB300 its per-row staging,
-         * and in a batch the larger staging area of every job, cost more than
-         * it saves, except on large grids evaluated alone: measured -17 % on
-         * the 256 x 256 grid (diameter 140), +5 % to +21 % on single grids of
-         * 64 x 64 to 180 x 180 and +8 % on the 512-graph batch.  So by default
-         * it is on only for a single grid of at least 49152 vertices. */
-        int act;
-        if(tuning->activity == -2) act = count == 1 && g->grid && g->n >= 49152;
-        else act = tuning->activity == -1 ? g->grid : tuning->activity;
-        j->flags = act ? GBX_JOB_ACTIVE : 0;
+        j->flags = tracks_changes(tuning, count, g->grid, g->n) ? GBX_JOB_ACTIVE : 0;
         ord[k].job = k;
         ord[k].work = (double)g->n * wc * (g->d + 2) * (count > 1 ? 1.0 : 0.0);
       }
@@ -389,7 +400,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   /* Slots: for batches, as many concurrent jobs as the L2 budget holds, at
    * least 64; for a single graph a fixed count measured best on GB300 (4 for
    * general graphs; 8 for grids, whose many short levels leave hand-offs to
-   * hide).  Capped by the job count. */
+   * hide, 16 for grids with change tracking).  Capped by the job count. */
   size_t max_words = 0, max_rows = 0;
   double sum_fp = 0;
   int fit = 0;
@@ -403,7 +414,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   int nslots = tuning->slots > 0 ? tuning->slots : fit;
   if(tuning->slots <= 0){
     if(nslots < 2) nslots = 2;
-    if(count == 1) nslots = shapes[0].grid ? 8 : 4;
+    if(count == 1){
+      const int n0 = shapes[0].grid ? shapes[0].width * shapes[0].height : shapes[0].nodes;
+      nslots = !shapes[0].grid ? 4 : tracks_changes(tuning, 1, 1, n0) ? 16 : 8;
+    }
     if(count > 1 && nslots < 64) nslots = 64;
     if(nslots > 512) nslots = 512;
   }
