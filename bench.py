@@ -233,7 +233,7 @@ def serving(seconds, rate=20000.0):
     srv = og.Server(lanes=4, max_batch=16, max_nodes=32768, memory_mb=4096)
     handles = [srv.register(og.GraphSpec(s.adjacency.copy(), nodes=s.nodes)) for s in specs]
     think_mean = len(shapes) / rate
-    lat, done = [], [0]
+    lat, done, lat_by_n = [], [0], {}
     lock = threading.Lock()
     stop_at = [0.0]
     checks = []
@@ -261,6 +261,7 @@ def serving(seconds, rate=20000.0):
         srv.wait(srv.submit(handles[k], undo))
         with lock:
             lat.extend(local)
+            lat_by_n.setdefault(n, []).extend(local)
             done[0] += len(local)
             if k < 4:
                 checks.append((k, host, res))
@@ -295,6 +296,9 @@ def serving(seconds, rate=20000.0):
             "offered_cap_req_per_s": rate,
             "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
                            "mean": float(lat_ms.mean())},
+            "latency_ms_by_n": {str(k): {"p50": float(np.percentile(np.array(v) * 1e3, 50)),
+                                         "p99": float(np.percentile(np.array(v) * 1e3, 99)), "requests": len(v)}
+                                for k, v in sorted(lat_by_n.items())},
             "batches": st["batches"], "mean_batch": st["batched_requests"] / max(1, st["batches"]),
             "max_batch": st["max_batch"], "max_concurrent_lanes": st["max_inflight_lanes"],
             "per_call_evals_per_s_same_mix": 1.0 / float(np.mean(pc)),

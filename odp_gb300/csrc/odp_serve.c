@@ -37,6 +37,7 @@
 typedef struct {
   int grid, grid_s, n, d, dp, s, B, W, width, height;
   int wc_log2, nchunks, tile_rows, ntiles;
+  double cost;                 /* bytes one level of all its chunks moves: the batching class */
   int *d_adj, *d_nbr, *d_ndeg, *d_itable;
   gbx_expand_desc *d_desc;
   int *h_adj;                  /* host mirror of the compact adjacency */
@@ -217,16 +218,18 @@ static void finish_batch(odp_server *s, serve_lane *l)
 static int launch_batch(odp_server *s, serve_lane *l)
 {
   int nreq = 0, njobs = 0, nw = 0;
-  long long first_open = -1;
+  double seed_cost = 0;
   for(long long id = s->next_pending; id < s->nreqs && nreq < l->max_batch; id++){
     serve_req *r = &s->reqs[id];
     if(r->state != 0) continue;
     serve_graph *g = &s->graphs[r->graph];
     int need_w = r->ndelta * (1 + g->s);
-    if(g->busy || njobs + g->nchunks > l->max_jobs || nw + need_w > l->max_writes){
-      if(first_open < 0) first_open = id;
-      continue;
-    }
+    /* A batch holds requests of similar cost (within 4x of the oldest one it
+     * takes): a request completes only when its whole batch does, so a small
+     * graph batched with a large one would wait for it. */
+    int other_class = nreq > 0 && (g->cost > 4.0 * seed_cost || 4.0 * g->cost < seed_cost);
+    if(g->busy || other_class || njobs + g->nchunks > l->max_jobs || nw + need_w > l->max_writes) continue;
+    if(nreq == 0) seed_cost = g->cost;
     for(int k = 0; k < r->ndelta; k++) nw += delta_writes(g, &r->deltas[k], l->h_writes + nw);
     free(r->deltas);
     r->deltas = NULL;
@@ -437,6 +440,7 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
     if(g.tile_rows > n) g.tile_rows = n;
   }
   g.ntiles = (n + g.tile_rows - 1) / g.tile_rows;
+  g.cost = level_bytes * g.nchunks;
   if(g.nchunks > s->lanes[0].max_jobs) return ODPX_ERR_MEMORY;   /* one request must fit a batch */
   size_t adj_ints = (size_t)g.B * g.d;
   g.h_adj = malloc(sizeof(int) * adj_ints);
