@@ -28,6 +28,7 @@
 #include <float.h>
 #include <pthread.h>
 #include <time.h>
+#include <math.h>
 #include <sys/prctl.h>
 #include "odp_plan.h"
 #include "odp_gb300.h"
@@ -87,6 +88,7 @@ struct odp_server {
   long long nreqs, cap_reqs, next_pending;
   serve_lane *lanes;
   double l2_lane_bytes;        /* bitset working set a lane keeps active at once (L2 share) */
+  double min_cost, max_cost;   /* over the registered graphs */
   ODPX_Serve_counters stats;
 };
 
@@ -215,7 +217,7 @@ static void finish_batch(odp_server *s, serve_lane *l)
 
 /* Forms a batch from the oldest pending requests whose graphs are idle and
  * launches it on lane l.  Called with the mutex held. */
-static int launch_batch(odp_server *s, serve_lane *l)
+static int launch_batch(odp_server *s, serve_lane *l, double max_seed_cost)
 {
   int nreq = 0, njobs = 0, nw = 0;
   double seed_cost = 0;
@@ -227,7 +229,8 @@ static int launch_batch(odp_server *s, serve_lane *l)
     /* A batch holds requests of similar cost (within 4x of the oldest one it
      * takes): a request completes only when its whole batch does, so a small
      * graph batched with a large one would wait for it. */
-    int other_class = nreq > 0 && (g->cost > 4.0 * seed_cost || 4.0 * g->cost < seed_cost);
+    int other_class = nreq > 0 ? (g->cost > 4.0 * seed_cost || 4.0 * g->cost < seed_cost)
+                               : g->cost > max_seed_cost;
     if(g->busy || other_class || njobs + g->nchunks > l->max_jobs || nw + need_w > l->max_writes) continue;
     if(nreq == 0) seed_cost = g->cost;
     for(int k = 0; k < r->ndelta; k++) nw += delta_writes(g, &r->deltas[k], l->h_writes + nw);
@@ -330,9 +333,13 @@ static void *scheduler(void *arg)
     }
     if(progress) pthread_cond_broadcast(&s->cv_done);
     int have_pending = s->next_pending < s->nreqs;
+    /* With several lanes, lane 0 takes only the cheaper half of the cost
+     * range (below the geometric mean of the registered graphs' costs), so
+     * small requests always find a lane that large batches cannot hold. */
+    const double small = s->cfg.lanes > 1 ? sqrt(s->min_cost * s->max_cost) : HUGE_VAL;
     for(int i = 0; i < s->cfg.lanes && have_pending; i++){
       serve_lane *l = &s->lanes[i];
-      if(!l->busy && launch_batch(s, l) > 0) progress = 1;
+      if(!l->busy && launch_batch(s, l, i == 0 ? small : HUGE_VAL) > 0) progress = 1;
       have_pending = s->next_pending < s->nreqs;
     }
     int inflight = 0;
@@ -513,6 +520,8 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
     s->graphs = realloc(s->graphs, sizeof(serve_graph) * (size_t)s->cap_graphs);
   }
   s->graphs[s->ngraphs] = g;
+  if(s->ngraphs == 0 || g.cost < s->min_cost) s->min_cost = g.cost;
+  if(s->ngraphs == 0 || g.cost > s->max_cost) s->max_cost = g.cost;
   *handle = s->ngraphs++;
   pthread_mutex_unlock(&s->mu);
   return 0;
