@@ -451,23 +451,44 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
   return cnt;
 }
 
-/* Takes one tile from the first slot (from `cursor` on) that has one left.
- * The ticket is read before it is incremented, so slots without tiles are
- * never pushed past their tile count by idle CTAs.  Thread 0 only. */
+/* Warp 0 takes one tile from the first slot (from `cursor` on) that has one
+ * left.  Each lane reads the tickets of up to four slots, so 128 slots cost
+ * one L2 round trip; the candidates are then tried in slot order, one atomic
+ * at a time.  A ticket is read before it is incremented, so slots without
+ * tiles are never pushed past their tile count by idle CTAs.  Every lane of
+ * warp 0 calls this and gets the same answer. */
 __device__ __forceinline__ bool take_tile(gbx_slot *slots, int nslots, int &cursor, int &slot, int &tile)
 {
-  for(int i = 0; i < nslots; i++){
-    int si = cursor + i;
-    if(si >= nslots) si -= nslots;
-    gbx_slot *sl = &slots[si];
-    unsigned long long t = vload(&sl->ticket);
-    if((unsigned)t >= (unsigned)(t >> 32)) continue;
-    t = atomicAdd(&sl->ticket, 1ull);
-    if((unsigned)t >= (unsigned)(t >> 32)) continue;
-    slot = si;
-    tile = (int)(unsigned)t;
-    cursor = si;
-    return true;
+  const int lane = threadIdx.x & 31;
+  for(int base = 0; base < nslots; base += 128){
+    unsigned long long t[4];
+    int si[4];
+#pragma unroll
+    for(int k = 0; k < 4; k++){
+      const int i = base + k * 32 + lane;
+      int s = cursor + i;
+      if(s >= nslots) s -= nslots;
+      si[k] = s;
+      t[k] = i < nslots ? vload(&slots[s].ticket) : 0ull;
+    }
+#pragma unroll
+    for(int k = 0; k < 4; k++){
+      unsigned m = __ballot_sync(0xffffffffu, (unsigned)t[k] < (unsigned)(t[k] >> 32));
+      while(m){
+        const int l = __ffs(m) - 1;
+        const int s = __shfl_sync(0xffffffffu, si[k], l);
+        unsigned long long r = 0;
+        if(lane == 0) r = atomicAdd(&slots[s].ticket, 1ull);
+        r = __shfl_sync(0xffffffffu, r, 0);
+        if((unsigned)r < (unsigned)(r >> 32)){
+          slot = s;
+          tile = (int)(unsigned)r;
+          cursor = s;
+          return true;
+        }
+        m &= m - 1;
+      }
+    }
   }
   return false;
 }
@@ -491,37 +512,40 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   if(blockIdx.x == 0 && threadIdx.x == 0) ctrl->t_start = globaltimer();
 
   for(;;){
-    if(threadIdx.x == 0){
-      int state = 0, slot = -1, tile = 0;
-      if(take_tile(slots, nslots, cursor, slot, tile)) state = 1;
-      if(state == 1){
-        __threadfence();                               /* acquire the level's inputs */
-        gbx_slot *sl = &slots[slot];
-        sh_slot = slot;
-        sh_tile = tile;
-        sh_level = vload(&sl->level);
-        sh_job = jobs[vload(&sl->job)];
-        sh_buf0 = vload(&sl->buf0);
-        sh_buf1 = vload(&sl->buf1);
-        sh_mask0 = vload(&sl->mask0);
-        sh_mask1 = vload(&sl->mask1);
-        idle_since = 0;
-      }
-      else{
-        if(vload(&ctrl->retired) >= (unsigned)nslots || (vload(&ctrl->error) & GBX_ERR_TIMEOUT)){
-          state = 2;
+    if(threadIdx.x < 32){
+      int slot = -1, tile = 0;
+      const bool got = take_tile(slots, nslots, cursor, slot, tile);
+      if(threadIdx.x == 0){
+        int state = got ? 1 : 0;
+        if(state == 1){
+          __threadfence();                               /* acquire the level's inputs */
+          gbx_slot *sl = &slots[slot];
+          sh_slot = slot;
+          sh_tile = tile;
+          sh_level = vload(&sl->level);
+          sh_job = jobs[vload(&sl->job)];
+          sh_buf0 = vload(&sl->buf0);
+          sh_buf1 = vload(&sl->buf1);
+          sh_mask0 = vload(&sl->mask0);
+          sh_mask1 = vload(&sl->mask1);
+          idle_since = 0;
         }
         else{
-          unsigned long long now = globaltimer();
-          if(idle_since == 0) idle_since = now;
-          if(now - idle_since > spin_limit_ns){
-            atomicOr(&ctrl->error, GBX_ERR_TIMEOUT);
+          if(vload(&ctrl->retired) >= (unsigned)nslots || (vload(&ctrl->error) & GBX_ERR_TIMEOUT)){
             state = 2;
           }
-          else __nanosleep(256);
+          else{
+            unsigned long long now = globaltimer();
+            if(idle_since == 0) idle_since = now;
+            if(now - idle_since > spin_limit_ns){
+              atomicOr(&ctrl->error, GBX_ERR_TIMEOUT);
+              state = 2;
+            }
+            else __nanosleep(256);
+          }
         }
+        sh_state = state;
       }
-      sh_state = state;
     }
     __syncthreads();
     const int state = sh_state;
