@@ -501,6 +501,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   __shared__ int sh_state, sh_slot, sh_tile, sh_level;
   __shared__ unsigned long long *sh_buf0, *sh_buf1;
   __shared__ unsigned *sh_mask0, *sh_mask1;
+  __shared__ __align__(16) gbx_slot sh_head;        /* head of the slot taken */
   __shared__ unsigned sh_warp[ENGINE_WARPS];
   /* Staging area in dynamic shared memory: the launch gives the whole Stage
    * when some job tracks changes, else only its index block. */
@@ -515,19 +516,26 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
     if(threadIdx.x < 32){
       int slot = -1, tile = 0;
       const bool got = take_tile(slots, nslots, cursor, slot, tile);
+      if(got){
+        /* acquire the level's inputs, then read the slot's head (its level,
+         * buffers and job descriptor) with one 16-byte load per lane */
+        __threadfence();
+        const int lane = threadIdx.x;
+        if(lane < GBX_SLOT_HEAD_BYTES / 16)
+          reinterpret_cast<uint4 *>(&sh_head)[lane] = __ldcg(reinterpret_cast<const uint4 *>(slots + slot) + lane);
+        __syncwarp();
+      }
       if(threadIdx.x == 0){
         int state = got ? 1 : 0;
         if(state == 1){
-          __threadfence();                               /* acquire the level's inputs */
-          gbx_slot *sl = &slots[slot];
           sh_slot = slot;
           sh_tile = tile;
-          sh_level = vload(&sl->level);
-          sh_job = jobs[vload(&sl->job)];
-          sh_buf0 = vload(&sl->buf0);
-          sh_buf1 = vload(&sl->buf1);
-          sh_mask0 = vload(&sl->mask0);
-          sh_mask1 = vload(&sl->mask1);
+          sh_level = sh_head.level;
+          sh_job = sh_head.desc;
+          sh_buf0 = sh_head.buf0;
+          sh_buf1 = sh_head.buf1;
+          sh_mask0 = sh_head.mask0;
+          sh_mask1 = sh_head.mask1;
           idle_since = 0;
         }
         else{
@@ -625,6 +633,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
               const gbx_job nj = jobs[j];
               job_out[j].t_loaded = globaltimer();
               sl->job = (int)j;
+              sl->desc = nj;
               sl->level = 1;
               sl->count = 0;
               sl->done = 0;
@@ -1039,6 +1048,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   for(int k = 0; k < nslots; k++){
     sl[k].ticket = (unsigned long long)jobs[k].ntiles << 32;
     sl[k].job = k;
+    sl[k].desc = jobs[k];
     sl[k].level = 1;
     sl[k].prev = (unsigned long long)jobs[k].nsrc;
     sl[k].sum = ((long long)n * jobs[k].nsrc - jobs[k].nsrc) * s;

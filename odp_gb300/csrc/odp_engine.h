@@ -47,7 +47,9 @@ typedef struct {
 
 #define GBX_JOB_ACTIVE 1
 
-/* Per-slot mutable state, one 128-byte line each. */
+/* Per-slot mutable state, two 128-byte lines each.  The slot holds a copy
+ * of its job's descriptor, so a CTA that takes a tile reads everything it
+ * needs from the slot's first 144 bytes in one round trip. */
 typedef struct {
   unsigned long long ticket;   /* (ntiles << 32) | next tile */
   unsigned int done;           /* tiles finished at the current level */
@@ -59,8 +61,16 @@ typedef struct {
   long long sum;               /* this job's share of the ordered distance sum */
   unsigned long long *buf0, *buf1;
   unsigned int *mask0, *mask1; /* per row: which lanes' words changed at a level */
-  unsigned long long pad1[6];
+  gbx_job desc;                /* jobs[job], written before the ticket that publishes it */
+  unsigned long long pad1[14];
 } gbx_slot;
+
+#define GBX_SLOT_HEAD_BYTES 144  /* ticket .. desc: what a CTA taking a tile reads */
+#ifdef __cplusplus
+static_assert(sizeof(gbx_job) == 64 && sizeof(gbx_slot) == 256, "slot layout");
+#else
+_Static_assert(sizeof(gbx_job) == 64 && sizeof(gbx_slot) == 256, "slot layout");
+#endif
 
 typedef struct {
   unsigned int next_job;       /* next job index to load into a freed slot */

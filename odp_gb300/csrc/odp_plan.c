@@ -220,6 +220,7 @@ static void fill_state_init(odp_plan *p)
     const gbx_job *j = &p->h_jobs[k];
     sl[k].ticket = (unsigned long long)j->ntiles << 32;
     sl[k].job = k;
+    sl[k].desc = *j;
     sl[k].level = 1;
     sl[k].prev = (unsigned long long)j->nsrc;
     sl[k].sum = ((long long)j->n * j->nsrc - j->nsrc) * j->sym;

@@ -271,6 +271,7 @@ static int launch_batch(odp_server *s, serve_lane *l, double max_seed_cost)
     const gbx_job *j = &l->h_jobs[k];
     sl[k].ticket = (unsigned long long)j->ntiles << 32;
     sl[k].job = k;
+    sl[k].desc = *j;
     sl[k].level = 1;
     sl[k].prev = (unsigned long long)j->nsrc;
     sl[k].sum = ((long long)j->n * j->nsrc - j->nsrc) * j->sym;
