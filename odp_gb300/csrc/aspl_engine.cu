@@ -38,6 +38,7 @@
  *    by the CTA that took it, with no device-wide handshake per level.
  */
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 #include "odp_engine.h"
 
@@ -212,15 +213,31 @@ __device__ __forceinline__ void mark_source(uint4 (&acc)[RowShape<WC>::V], int b
 #define IDX_SMEM_INTS 4096
 #define BLOCK_ROWS_MAX (IDX_SMEM_INTS / 4)
 
-/* Per-block staging area: the block's neighbour lists, the previous level's
- * change masks of those neighbours, and per row its own previous mask and
- * the union of both (rows whose lanes have nothing to do are skipped). */
+/* Per-block staging area: the block's neighbour lists and two per-row lane
+ * masks.  Without change tracking, `own` holds the lanes whose words were
+ * saturated (every source bit of the lane set) at the previous level and
+ * `act` those saturated two levels back.  With change tracking, `nmask`
+ * holds the previous level's change masks of the neighbours, `own` the row's
+ * own and `act` the union of both (rows whose lanes have nothing to do are
+ * skipped).  Launches without change tracking get the area up to `nmask`. */
 struct Stage {
   int idx[IDX_SMEM_INTS];
-  unsigned nmask[IDX_SMEM_INTS];
   unsigned own[BLOCK_ROWS_MAX];
   unsigned act[BLOCK_ROWS_MAX];
+  unsigned nmask[IDX_SMEM_INTS];
 };
+
+/* Source bits a lane holds in one row of a chunk of nsrc sources: its
+ * vectors gl, gl + G, ... each cover 128 source ordinals. */
+template <int WC>
+__device__ __forceinline__ int lane_sources(int nsrc, int gl)
+{
+  typedef RowShape<WC> S;
+  int v = 0;
+#pragma unroll
+  for(int k = 0; k < S::V; k++) v += min(max(nsrc - 128 * (gl + k * S::G), 0), 128);
+  return v;
+}
 
 /* Source ordinal of a row (the bit it owns across the chunks): the row
  * itself, or from the graph's source table (SP). */
@@ -263,68 +280,90 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
         mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.w) - src0, nsrc, gl);
       }
       uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
+      unsigned c = 0;
 #pragma unroll
       for(int k = 0; k < S::V; k++){
         __stcg(yr + k * S::G, acc[k]);
-        cnt += popc4(acc[k]);
+        c += popc4(acc[k]);
         if(ACT)
           changed |= (acc[k].x != id[k].x) | (acc[k].y != id[k].y) | (acc[k].z != id[k].z) |
                      (acc[k].w != id[k].w);
       }
+      cnt += c;
+      if(!ACT) changed = c == (unsigned)lane_sources<WC>(nsrc, gl);    /* saturated */
     }
-    if(ACT){
-      const unsigned bal = __ballot_sync(0xffffffffu, changed);
-      if(valid && gl == 0)
-        Mcur[row0 + r] = S::G == 32 ? bal : (bal >> (sub * S::G)) & ((1u << S::G) - 1u);
-    }
+    const unsigned bal = __ballot_sync(0xffffffffu, changed);
+    if(valid && gl == 0)
+      Mcur[row0 + r] = S::G == 32 ? bal : (bal >> (sub * S::G)) & ((1u << S::G) - 1u);
   }
   return cnt;
 }
 
 /* Level k >= 2 without change tracking: P_k[v] = P_{k-1}[v] | OR_j
- * P_{k-1}[nbr[v][j]] over the d neighbour columns, every word written.
- * Eight 16-byte loads per lane are in flight per step (NB neighbours x V
- * vectors).  Columns that hold no neighbour hold the row itself, so only the
- * step past the last column needs a test.  Returns the bits set at this
- * level. */
+ * P_{k-1}[nbr[v][j]] over the d neighbour columns.  Eight 16-byte loads per
+ * lane are in flight per step (NB neighbours x V vectors).  Columns that
+ * hold no neighbour hold the row itself, so only the step past the last
+ * column needs a test.  A lane whose words were saturated at level k-1 stays
+ * so: it gathers nothing, and copies its words from X only if they were not
+ * already saturated at level k-2 (Y then still holds them).  Lanes past the chunk's
+ * last source are saturated from level 1 on.  Returns the bits set at this
+ * level; the row's saturated lanes replace its entry of `own` (the group's
+ * lanes have all read it before the ballot). */
 template <int WC>
-__device__ unsigned rows_levelk_all(const Stage &st, int dp, int d, const unsigned long long *X, unsigned long long *Y,
-                                    int row0, int nrows)
+__device__ unsigned rows_levelk_all(Stage &st, int dp, int d, int nsrc, const unsigned long long *X,
+                                    unsigned long long *Y, int row0, int nrows)
 {
   typedef RowShape<WC> S;
   constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
+  const unsigned lane_bits = (unsigned)lane_sources<WC>(nsrc, gl);
   const uint4 *Xv = reinterpret_cast<const uint4 *>(X);
   unsigned cnt = 0;
   for(int r = warp * S::RPW + sub; r < nrows; r += ENGINE_WARPS * S::RPW){
     const int row = row0 + r;
-    uint4 acc[S::V];
-    const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
-#pragma unroll
-    for(int k = 0; k < S::V; k++) acc[k] = __ldcg(xr + k * S::G);
-    const int *ip = st.idx + r * dp;
-    for(int j = 0; j < d; j += NB){
-      uint4 t[NB][S::V];
-#pragma unroll
-      for(int i = 0; i < NB; i++){
-        const bool ok = j + i < d;
-        const uint4 *nr = Xv + (size_t)ip[ok ? j + i : j] * S::VPR + gl;
+    uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
+    bool sat = (st.own[r] >> gl) & 1u;
+    if(sat){
+      if(!((st.act[r] >> gl) & 1u)){
 #pragma unroll
         for(int k = 0; k < S::V; k++)
-          t[i][k] = ok ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+          __stcg(yr + k * S::G, __ldcg(Xv + (size_t)row * S::VPR + gl + k * S::G));
       }
-#pragma unroll
-      for(int i = 0; i < NB; i++)
-#pragma unroll
-        for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
+      cnt += lane_bits;
     }
-    uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
+    else{
+      uint4 acc[S::V];
+      const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
 #pragma unroll
-    for(int k = 0; k < S::V; k++){
-      __stcg(yr + k * S::G, acc[k]);
-      cnt += popc4(acc[k]);
+      for(int k = 0; k < S::V; k++) acc[k] = __ldcg(xr + k * S::G);
+      const int *ip = st.idx + r * dp;
+      for(int j = 0; j < d; j += NB){
+        uint4 t[NB][S::V];
+#pragma unroll
+        for(int i = 0; i < NB; i++){
+          const bool ok = j + i < d;
+          const uint4 *nr = Xv + (size_t)ip[ok ? j + i : j] * S::VPR + gl;
+#pragma unroll
+          for(int k = 0; k < S::V; k++)
+            t[i][k] = ok ? __ldcg(nr + k * S::G) : make_uint4(0u, 0u, 0u, 0u);
+        }
+#pragma unroll
+        for(int i = 0; i < NB; i++)
+#pragma unroll
+          for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
+      }
+      unsigned c = 0;
+#pragma unroll
+      for(int k = 0; k < S::V; k++){
+        __stcg(yr + k * S::G, acc[k]);
+        c += popc4(acc[k]);
+      }
+      cnt += c;
+      sat = c == lane_bits;
     }
+    const unsigned bal = __ballot_sync(S::G == 32 ? 0xffffffffu : (((1u << S::G) - 1u) << (sub * S::G)), sat);
+    if(gl == 0) st.own[r] = S::G == 32 ? bal : (bal >> (sub * S::G)) & ((1u << S::G) - 1u);
   }
   return cnt;
 }
@@ -396,7 +435,7 @@ __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long lon
 }
 
 template <int WC>
-__device__ unsigned run_block(const Stage &st, int dp, const gbx_job &jb, int level, const unsigned long long *X,
+__device__ unsigned run_block(Stage &st, int dp, const gbx_job &jb, int level, const unsigned long long *X,
                               unsigned long long *Y, unsigned *Mcur, int row0, int nrows)
 {
   if(jb.flags & GBX_JOB_ACTIVE){
@@ -404,7 +443,7 @@ __device__ unsigned run_block(const Stage &st, int dp, const gbx_job &jb, int le
     return jb.srcpos ? rows_level1<WC, true, true>(st, dp, jb, Y, Mcur, row0, nrows)
                      : rows_level1<WC, true, false>(st, dp, jb, Y, Mcur, row0, nrows);
   }
-  if(level > 1) return rows_levelk_all<WC>(st, dp, jb.d, X, Y, row0, nrows);
+  if(level > 1) return rows_levelk_all<WC>(st, dp, jb.d, jb.nsrc, X, Y, row0, nrows);
   return jb.srcpos ? rows_level1<WC, false, true>(st, dp, jb, Y, Mcur, row0, nrows)
                    : rows_level1<WC, false, false>(st, dp, jb, Y, Mcur, row0, nrows);
 }
@@ -424,6 +463,14 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
     const int4 *src = reinterpret_cast<const int4 *>(jb.nbr + (size_t)b0 * dp);
     int4 *dst = reinterpret_cast<int4 *>(st.idx);
     for(int i = threadIdx.x; i < (nr * dp) >> 2; i += ENGINE_THREADS) dst[i] = __ldg(src + i);
+    if(level > 1 && !(jb.flags & GBX_JOB_ACTIVE)){
+      /* saturated lanes at k-1, and at k-2 (Mcur still holds that level's
+       * masks; at level 2 it holds nothing of this job) */
+      for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS){
+        st.own[r] = __ldcg(Mprev + b0 + r);
+        st.act[r] = level >= 3 ? __ldcg(Mcur + b0 + r) : 0u;
+      }
+    }
     if(level > 1 && (jb.flags & GBX_JOB_ACTIVE)){
       for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS) st.own[r] = __ldcg(Mprev + b0 + r);
       __syncthreads();
@@ -447,6 +494,10 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
     }
 #undef ODP_WC_CASE
     __syncthreads();
+    /* saturation masks of this level out; each thread copies the entries it
+     * staged, so the next block's staging needs no barrier first */
+    if(level > 1 && !(jb.flags & GBX_JOB_ACTIVE))
+      for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS) __stcg(Mcur + b0 + r, st.own[r]);
   }
   return cnt;
 }
@@ -687,7 +738,7 @@ __global__ void scatter_kernel(const gbx_write *__restrict__ w, int count)
 int g_engine_blocks = 0, g_engine_blocks_active = 0;
 int g_pageable_access = 0;
 
-constexpr size_t STAGE_BYTES_PLAIN = sizeof(int) * IDX_SMEM_INTS;
+constexpr size_t STAGE_BYTES_PLAIN = offsetof(Stage, nmask);
 constexpr size_t STAGE_BYTES_ACTIVE = sizeof(Stage);
 
 }  // namespace
