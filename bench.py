@@ -51,10 +51,14 @@ METRIC = "ASPL evals/s, batched vs per-call on 1 GB300 (bit-exact)"
 C2 = dict(nodes=65536, degree=16, seed=2, sha256="d855fb662f9e9557", result=(6, 9346294313))
 WORKLOAD = ("batched: 512 graphs, seeds 100..611, n log-uniform [256, 8192], d in {4..32}, "
             "80% general / 20% grid (length 3-6), s in {1,2,4}")
-# DRAM traffic of one engine_kernel launch (dram__bytes_read.sum + dram__bytes_write.sum, one ncu capture,
-# profiles/engine_kernel_batch.md) on the first 128 graphs of the batch, with that launch's algorithmic
-# bytes.  A full batch launch's traffic is taken as this scaled by algorithmic bytes.
-NCU_DRAM = {"bytes": 992011264.0 + 934300160.0, "bytes_alg": 24803482864.0, "graphs": 128}
+# One ncu capture of an engine_kernel launch on the first 128 graphs of the batch
+# (profiles/engine_kernel_batch.md): DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum), bytes
+# read from L2 by the SMs (l1tex__m_xbar2l1tex_read_bytes.sum), and that launch's algorithmic bytes.  A full
+# batch launch's figures are taken as these scaled by algorithmic bytes.  The engine reads fewer bytes than
+# the algorithmic count: level 1 is built from the neighbour lists, and lanes whose words are saturated
+# gather nothing.
+NCU_DRAM = {"bytes": 936275200.0 + 815841024.0, "l2_read_bytes": 14874844864.0, "bytes_alg": 24803482864.0,
+            "graphs": 128}
 
 
 def parse():
@@ -493,6 +497,11 @@ def run_own(args):
                                           "bytes" % NCU_DRAM["graphs"],
                         "bytes_alg_per_launch": balg, "l2_read_peak_measured": l2,
                         "frac_of_l2_read_peak": achieved / l2 if l2 > 0 else None}
+    moved = NCU_DRAM["l2_read_bytes"] * balg / NCU_DRAM["bytes_alg"]
+    line["roofline"].update({"l2_read_bytes_per_launch": moved, "l2_read_gbs": moved / (ms * 1e-3) / 1e9,
+                             "l2_read_frac_of_l2_read_peak": moved / (ms * 1e-3) / 1e9 / l2 if l2 > 0 else None,
+                             "l2_read_source": "ncu L2-to-SM read bytes of one launch on the first %d graphs, scaled "
+                                               "by algorithmic bytes" % NCU_DRAM["graphs"]})
     line["clocks"] = clk.summary()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, done, dt, cres, cores = oracle_sample(specs, args.cpu_seconds)

@@ -234,15 +234,20 @@ static void fill_state_init(odp_plan *p)
 }
 
 /* Whether a graph's jobs track changes (gather only words that changed at
- * the previous level).  It is exact for every graph.  On GB300 its per-row
- * staging, and in a batch the larger staging area of every job, cost more
- * than it saves, except on large grids evaluated alone: measured -17 % on the
- * 256 x 256 grid (diameter 140), +5 % to +21 % on single grids of 64 x 64 to
- * 180 x 180 and +8 % on the 512-graph batch.  So by default it is on only
- * for a single grid of at least 49152 vertices. */
-static int tracks_changes(const odp_tuning *t, int count, int grid, int n)
+ * the previous level).  It is exact for every graph.  Without it, lanes whose
+ * words are saturated already skip their gathers, and on GB300 the per-row
+ * staging of change tracking, and in a batch the larger staging area of
+ * every job, cost more than it saves, except on large grids with many
+ * sources evaluated alone.  Measured against the saturation skip alone:
+ * 256 x 256 grid, d = 6, diameter 140: 28.3 -> 25.3 ms; 224 x 224: 18.2 ->
+ * 15.7 ms; 256 x 256, d = 8, s = 2 (32768 sources): 9.7 -> 9.1 ms; but
+ * 256 x 256, s = 4 (16384 sources, so only four 64-word jobs): 7.3 -> 8.2 ms;
+ * and before the skip already +5 % to +21 % on single grids of 64 x 64 to
+ * 180 x 180 and +8 % on the 512-graph batch.  So by default it is on only for
+ * a single grid of at least 49152 vertices and 32768 sources. */
+static int tracks_changes(const odp_tuning *t, int count, int grid, int n, int s)
 {
-  if(t->activity == -2) return count == 1 && grid && n >= 49152;
+  if(t->activity == -2) return count == 1 && grid && n >= 49152 && n / s >= 32768;
   return t->activity == -1 ? grid : t->activity;
 }
 
@@ -288,7 +293,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     int wl;
     if(tuning->wc_log2 > 0) wl = tuning->wc_log2;
     else if(te && te->wc_log2 > 0) wl = te->wc_log2;
-    else if(tracks_changes(tuning, count, sh->grid, g->n)){
+    else if(tracks_changes(tuning, count, sh->grid, g->n, g->s)){
       /* 512-byte rows for a grid with change tracking (the 256 x 256 grid:
        * 24.4 ms with 64 words and 16 slots against 28.8 ms with 32 and 8) */
       wl = full_l2 < 6 ? full_l2 : 6;
@@ -334,7 +339,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       double lb = (double)g->n * (1 << g->wc_log2) * 8.0 * (g->d + 2);
       int conc = g->nchunks;
       if(count == 1){
-        int cap = !g->grid ? 4 : tracks_changes(tuning, 1, 1, g->n) ? 16 : 8;
+        int cap = !g->grid ? 4 : tracks_changes(tuning, 1, 1, g->n, g->s) ? 16 : 8;
         if(conc > cap) conc = cap;
       }
       active += lb * conc;
@@ -383,7 +388,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
         j->nsrc = g->B - j->src0 < wc * 64 ? g->B - j->src0 : wc * 64;
         j->sym = g->s; j->graph = i;
         j->tile_rows = g->tile_rows; j->ntiles = g->ntiles;
-        j->flags = tracks_changes(tuning, count, g->grid, g->n) ? GBX_JOB_ACTIVE : 0;
+        j->flags = tracks_changes(tuning, count, g->grid, g->n, g->s) ? GBX_JOB_ACTIVE : 0;
         ord[k].job = k;
         ord[k].work = (double)g->n * wc * (g->d + 2) * (count > 1 ? 1.0 : 0.0);
       }
@@ -417,7 +422,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     if(nslots < 2) nslots = 2;
     if(count == 1){
       const int n0 = shapes[0].grid ? shapes[0].width * shapes[0].height : shapes[0].nodes;
-      nslots = !shapes[0].grid ? 4 : tracks_changes(tuning, 1, 1, n0) ? 16 : 8;
+      nslots = !shapes[0].grid ? 4 : tracks_changes(tuning, 1, 1, n0, shapes[0].symmetries) ? 16 : 8;
     }
     if(count > 1 && nslots < 64) nslots = 64;
     if(nslots > 512) nslots = 512;
