@@ -164,6 +164,50 @@ def test_chunking_and_tiling_do_not_change_results(wc_log2, slots, tile_rows):
         og.set_tuning()
 
 
+def _saturation_cases():
+    """Graphs whose rows saturate early, or never, or hold padding lanes."""
+    cases = []
+    g = lambda n, d, s=1, seed=1: og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, s, seed=seed), d, s)
+    cases.append(og.GraphSpec(g(300, 40, seed=5), nodes=300))            # diameter 3: most lanes saturate at 2
+    cases.append(og.GraphSpec(g(1000, 12, seed=6), nodes=1000))          # 1000 sources: padding lanes past 1000
+    cases.append(og.GraphSpec(g(1000, 10, 4, seed=7), nodes=1000, symmetries=4))
+    irr = g(500, 8, seed=8)
+    u, v = 0, int(irr[0, 7])
+    j = int(np.nonzero(irr[v] == u)[0][0])
+    irr[v, j], irr[v, 7] = irr[v, 7], irr[v, j]
+    irr[u, 7] = irr[v, 7] = -1
+    deg = np.full(500, 8, dtype=np.int32)
+    deg[u] = deg[v] = 7
+    cases.append(og.GraphSpec(irr, nodes=500, num_degrees=deg))
+    half = g(128, 4, seed=9)                                             # two components: never saturates
+    cases.append(og.GraphSpec(np.concatenate([half, half + 128]).astype(np.int32), nodes=256))
+    e = og.generate_random_grid(30, 30, 6, 3, 1, seed=10)
+    cases.append(og.GraphSpec(og.conv_edge2adjacency_grid(30, 30, e, 6, 1), grid=True, width=30, height=30))
+    return cases
+
+
+@pytest.mark.parametrize("wc_log2", [1, 3, 5, 7])
+def test_saturated_lanes_skip_only_what_cannot_change(wc_log2):
+    """Lanes whose words hold every source bit of the chunk skip their
+    gathers.  Chunk widths of 2 to 128 words (1 to 32 lanes per row, one to
+    four vectors per lane), small multi-tile levels, and graphs that
+    saturate at level 2, hold padding lanes, are symmetric or irregular,
+    never saturate (disconnected) or are grids."""
+    cases = _saturation_cases()
+    refs = [oracle.aspl(c.adjacency, nodes=c.nodes, num_degrees=c.num_degrees, symmetries=c.symmetries,
+                        grid=c.grid, width=c.width, height=c.height) for c in cases]
+    assert refs[4][0] == 2147483647
+    og.set_tuning(wc_log2=wc_log2, slots=3, tile_rows=16, local_kb=1)
+    try:
+        b = og.Batch(cases)
+        got = b.run()
+        b.close()
+    finally:
+        og.set_tuning()
+    for k, (x, y) in enumerate(zip(got, refs)):
+        assert same(x, y), (k, x, y)
+
+
 def test_config1_default_kind_and_saving():
     n, d = 1024, 8
     adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=1), d)
