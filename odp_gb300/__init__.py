@@ -101,6 +101,7 @@ def load():
         "ODPX_Batch_job_profile": (I, [P, IP, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double), I]),
         "ODPX_Batch_set_wait_limit": (None, [P, ctypes.c_ulonglong]),
         "ODPX_Batch_bytes_alg": (ctypes.c_double, [P]),
+        "ODPX_Batch_kernel": (I, [P]),
         "ODPX_Measure_l2_read_gbs": (ctypes.c_double, [I, I]),
         "ODPX_Set_tuning": (None, [I, I, I, I, I, I]),
         "ODPX_Current_plan": (P, []),
@@ -472,6 +473,10 @@ class Batch:
         v = [ctypes.c_int() for _ in range(4)]
         _check(load().ODPX_Batch_info(self._h, graph, *[ctypes.byref(x) for x in v]), "ODPX_Batch_info")
         return dict(njobs=v[0].value, nslots=v[1].value, wc_log2=v[2].value, tile_rows=v[3].value)
+
+    def kernel(self):
+        """'small' when every job runs in the small-graph kernel, else 'engine'."""
+        return "small" if load().ODPX_Batch_kernel(self._h) == 1 else "engine"
 
     def job_levels(self):
         """Per-job finishing level of the last run (plan order; negative: stalled)."""

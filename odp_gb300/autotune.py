@@ -66,49 +66,60 @@ def measure(specs, repeats=3, flush_mb=256):
 
 
 def tune_batch(specs, slots=(32, 64, 128), local_kb=(256, 2048), widths=(3, 4, 5, 6, 7), tile_kb=(128, 640, 1280),
-               repeats=3, max_buckets=12):
+               repeats=3, max_buckets=12, rounds=2, min_gain=0.003):
     """Tunes a batch: a global pass over slots and the local-job threshold,
-    then a per-bucket pass over chunk widths and, for the chosen width, tile
-    traffic (buckets in order of their share of the work).  Installs and
+    then per-bucket passes over chunk widths and tile traffic (buckets in
+    order of their share of the work, up to `rounds` times), then the global
+    pass again with the table installed.  A trial replaces the current choice
+    only if it is faster by more than `min_gain` (a fraction): a greedy search
+    that follows timing noise can settle on a worse schedule.  Installs and
     returns the result."""
     t0 = time.perf_counter()
     clear()
+    og.set_tuning()
     base = measure(specs, repeats)
-    best = (base, 0, 0)
-    for sl in slots:
-        for lk in local_kb:
-            og.set_tuning(slots=sl, local_kb=lk)
-            ms = measure(specs, repeats)
-            if ms < best[0]:
-                best = (ms, sl, lk)
-    og.set_tuning(slots=best[1], local_kb=best[2])
+
+    def better(ms, cur):
+        return ms < cur * (1.0 - min_gain)
+
+    def global_pass(cur, sl0, lk0):
+        best = (cur, sl0, lk0)
+        for sl in slots:
+            for lk in local_kb:
+                if (sl, lk) == (sl0, lk0):
+                    continue
+                og.set_tuning(slots=sl, local_kb=lk)
+                ms = measure(specs, repeats)
+                if better(ms, best[0]):
+                    best = (ms, sl, lk)
+        og.set_tuning(slots=best[1], local_kb=best[2])
+        return best
+
+    current, sl_best, lk_best = global_pass(base, 0, 0)
     weight = {}
     for s in specs:
         n = s.width * s.height if s.grid else s.nodes
         weight[bucket(s)] = weight.get(bucket(s), 0.0) + float(n) * n / s.symmetries * (s.degree + 2)
     order = sorted(weight, key=lambda k: -weight[k])[:max_buckets]
     table = {}
-    current = best[0]
-    for bk in order:
-        choice = None
-        for wl in widths:
-            trial = dict(table)
-            trial[bk] = {"wc_log2": wl}
-            set_table(trial)
-            ms = measure(specs, repeats)
-            if ms < current:
-                current, choice = ms, {"wc_log2": wl}
-        if choice is not None:
-            table[bk] = choice
-        for tk in tile_kb:
-            trial = dict(table)
-            trial[bk] = dict(table.get(bk, {}), tile_kb=tk)
-            set_table(trial)
-            ms = measure(specs, repeats)
-            if ms < current:
-                current, table[bk] = ms, trial[bk]
-        set_table(table)
-    return {"default_ms": base, "tuned_ms": current, "slots": best[1], "local_kb": best[2],
+    for _ in range(rounds):
+        changed = False
+        for bk in order:
+            for key, values in (("wc_log2", widths), ("tile_kb", tile_kb)):
+                for v in values:
+                    if table.get(bk, {}).get(key) == v:
+                        continue
+                    trial = dict(table)
+                    trial[bk] = dict(table.get(bk, {}), **{key: v})
+                    set_table(trial)
+                    ms = measure(specs, repeats)
+                    if better(ms, current):
+                        current, table, changed = ms, trial, True
+                set_table(table)
+        if not changed:
+            break
+    current, sl_best, lk_best = global_pass(current, sl_best, lk_best)
+    return {"default_ms": base, "tuned_ms": current, "slots": sl_best, "local_kb": lk_best,
             "buckets": {"%d/%d/%d" % k: v for k, v in table.items()},
             "seconds": time.perf_counter() - t0}
 

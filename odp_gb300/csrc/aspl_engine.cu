@@ -712,6 +712,128 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
   }
 }
 
+/* ---------------------------------------------------------------------- */
+/* Small graphs: one CTA per job, both bitset buffers and the neighbour     */
+/* table in shared memory, every level in the CTA.                           */
+/* ---------------------------------------------------------------------- */
+
+#define SMALL_THREADS 512
+#define SMALL_WARPS (SMALL_THREADS / 32)
+
+/* One job (chunk of sources) of a graph whose level fits in shared memory.
+ * The same recurrence and bookkeeping as the engine: level 1 from the
+ * neighbour lists, then P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]], the
+ * bits set per level counted, the job complete when all n * nsrc bits are
+ * set and stalled when a level adds none (or the level reaches n). */
+template <int WC, bool SP>
+__device__ void small_job(const gbx_job &jb, int job, unsigned char *smem, gbx_graph_acc *acc,
+                          gbx_job_out *job_out)
+{
+  typedef RowShape<WC> S;
+  constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;
+  __shared__ unsigned long long s_cnt[2];
+  __shared__ int s_go;
+  const int n = jb.n, dp = jb.dp, d = jb.d, nsrc = jb.nsrc, src0 = jb.src0;
+  uint4 *b0 = reinterpret_cast<uint4 *>(smem);
+  uint4 *b1 = b0 + (size_t)n * S::VPR;
+  int *idx = reinterpret_cast<int *>(b1 + (size_t)n * S::VPR);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int sub = lane / S::G, gl = lane % S::G;
+
+  const int4 *src = reinterpret_cast<const int4 *>(jb.nbr);
+  for(int i = threadIdx.x; i < (n * dp) >> 2; i += SMALL_THREADS) reinterpret_cast<int4 *>(idx)[i] = __ldg(src + i);
+  if(threadIdx.x == 0){
+    s_cnt[0] = s_cnt[1] = 0;
+    job_out[job].t_loaded = globaltimer();
+  }
+  __syncthreads();
+
+  const unsigned long long full = (unsigned long long)n * (unsigned long long)nsrc;
+  unsigned long long prev = (unsigned long long)nsrc;                 /* thread 0's */
+  long long sum = ((long long)n * nsrc - nsrc) * jb.sym;               /* thread 0's */
+  for(int level = 1;; level++){
+    const uint4 *X = (level & 1) ? b0 : b1;
+    uint4 *Y = (level & 1) ? b1 : b0;
+    unsigned cnt = 0;
+    for(int r = warp * S::RPW + sub; r < n; r += SMALL_WARPS * S::RPW){
+      uint4 a[S::V];
+      const int *ip = idx + r * dp;
+      if(level == 1){
+#pragma unroll
+        for(int k = 0; k < S::V; k++) a[k] = make_uint4(0u, 0u, 0u, 0u);
+        mark_source<WC>(a, source_of<SP>(jb.srcpos, r) - src0, nsrc, gl);
+        for(int j = 0; j < dp; j++) mark_source<WC>(a, source_of<SP>(jb.srcpos, ip[j]) - src0, nsrc, gl);
+      }
+      else{
+#pragma unroll
+        for(int k = 0; k < S::V; k++) a[k] = X[(size_t)r * S::VPR + gl + k * S::G];
+        for(int j = 0; j < d; j += NB){
+          uint4 t[NB][S::V];
+#pragma unroll
+          for(int i = 0; i < NB; i++){
+            const bool ok = j + i < d;
+            const uint4 *nr = X + (size_t)ip[ok ? j + i : j] * S::VPR + gl;
+#pragma unroll
+            for(int k = 0; k < S::V; k++) t[i][k] = ok ? nr[k * S::G] : make_uint4(0u, 0u, 0u, 0u);
+          }
+#pragma unroll
+          for(int i = 0; i < NB; i++)
+#pragma unroll
+            for(int k = 0; k < S::V; k++) or_into(a[k], t[i][k]);
+        }
+      }
+#pragma unroll
+      for(int k = 0; k < S::V; k++){
+        Y[(size_t)r * S::VPR + gl + k * S::G] = a[k];
+        cnt += popc4(a[k]);
+      }
+    }
+    cnt = __reduce_add_sync(0xffffffffu, cnt);
+    if(lane == 0) atomicAdd(&s_cnt[level & 1], (unsigned long long)cnt);
+    __syncthreads();
+    if(threadIdx.x == 0){
+      const unsigned long long c = s_cnt[level & 1];
+      s_cnt[(level + 1) & 1] = 0;
+      const bool complete = c == full;
+      const bool stalled = !complete && (c == prev || level >= n);
+      int go = 0;
+      if(!complete && !stalled){
+        sum += (long long)(full - c) * jb.sym;
+        prev = c;
+        go = 1;
+      }
+      else{
+        gbx_graph_acc *ga = &acc[jb.graph];
+        job_out[job].level = stalled ? -level : level;
+        job_out[job].t_done = globaltimer();
+        atomicAdd(&ga->sum, (unsigned long long)sum);
+        atomicMax(&ga->levels, level);
+        if(stalled) atomicOr(&ga->flags, 1);
+      }
+      s_go = go;
+    }
+    __syncthreads();
+    if(!s_go) break;
+  }
+}
+
+__global__ void __launch_bounds__(SMALL_THREADS, 1)
+small_kernel(const gbx_job *__restrict__ jobs, gbx_graph_acc *acc, gbx_job_out *job_out)
+{
+  extern __shared__ __align__(16) unsigned char small_smem[];
+  const int job = blockIdx.x;
+  const gbx_job jb = jobs[job];
+#define ODP_SMALL_CASE(L) case L: \
+    if(jb.srcpos) small_job<(1 << L), true>(jb, job, small_smem, acc, job_out); \
+    else small_job<(1 << L), false>(jb, job, small_smem, acc, job_out); \
+    break;
+  switch(jb.wc_log2){
+    ODP_SMALL_CASE(1) ODP_SMALL_CASE(2) ODP_SMALL_CASE(3) ODP_SMALL_CASE(4)
+    default: break;
+  }
+#undef ODP_SMALL_CASE
+}
+
 /* L2 read ceiling for the roofline: every CTA streams an L2-resident buffer
  * with the same 16-byte ld.global.cg loads the engine uses, `reps` times. */
 __global__ void __launch_bounds__(256) l2_read_probe_kernel(const uint4 *__restrict__ buf, size_t vecs, int reps,
@@ -854,6 +976,26 @@ int gbx_memset(void *dst, int value, size_t bytes, void *stream)
 int gbx_stream_sync(void *stream) { return (int)cudaStreamSynchronize((cudaStream_t)stream); }
 
 const char *gbx_error_string(int err) { return cudaGetErrorString((cudaError_t)err); }
+
+int gbx_small_prepare(void)
+{
+  static int configured = 0;
+  if(configured) return 0;
+  cudaError_t e = cudaFuncSetAttribute(small_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       GBX_SMALL_SMEM_MAX);
+  if(e != cudaSuccess) return (int)e;
+  configured = 1;
+  return 0;
+}
+
+int gbx_small_launch(const gbx_job *d_jobs, int njobs, gbx_graph_acc *d_acc, gbx_job_out *d_job_out,
+                     size_t smem_bytes, void *stream)
+{
+  if(njobs <= 0) return 0;
+  if(smem_bytes > GBX_SMALL_SMEM_MAX) return (int)cudaErrorInvalidValue;
+  small_kernel<<<njobs, SMALL_THREADS, smem_bytes, (cudaStream_t)stream>>>(d_jobs, d_acc, d_job_out);
+  return (int)cudaGetLastError();
+}
 
 int gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream)
 {

@@ -98,6 +98,8 @@ int ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots,
   return 0;
 }
 
+int ODPX_Batch_kernel(const ODPX_Batch *batch) { return batch ? batch->small : ODPX_ERR_INVALID; }
+
 /* ODP_Set_aspl_batch keeps the last plan and reuses it (and its CUDA graph)
  * while the shapes and degree tables stay the same. */
 static struct {

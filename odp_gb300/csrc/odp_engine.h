@@ -47,6 +47,10 @@ typedef struct {
 
 #define GBX_JOB_ACTIVE 1
 
+/* Shared memory a job of the small-graph kernel may use: its two bitset
+ * buffers (2 x n x wc x 8 bytes) and its neighbour table (n x dp x 4). */
+#define GBX_SMALL_SMEM_MAX (200 * 1024)
+
 /* Per-slot mutable state, two 128-byte lines each.  The slot holds a copy
  * of its job's descriptor, so a CTA that takes a tile reads everything it
  * needs from the slot's first 144 bytes in one round trip. */
@@ -137,6 +141,14 @@ int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int 
 /* Copies every descriptor's host array `adj` into its `adj_dev` with
  * coalesced 16-byte loads over the CPU-GPU link (pageable host memory). */
 int  gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream);
+/* Jobs [0, njobs) of d_jobs, one CTA each, every level in shared memory
+ * (smem_bytes per CTA, at most GBX_SMALL_SMEM_MAX); results go to the same
+ * accumulators and per-job records as the engine's. */
+int  gbx_small_launch(const gbx_job *d_jobs, int njobs, gbx_graph_acc *d_acc, gbx_job_out *d_job_out,
+                      size_t smem_bytes, void *stream);
+/* Allows the small-graph kernel GBX_SMALL_SMEM_MAX bytes of shared memory
+ * (once per process; call before the first launch or capture). */
+int  gbx_small_prepare(void);
 
 /* Applies `count` writes, in stream order. */
 int  gbx_scatter(const gbx_write *d_writes, int count, void *stream);

@@ -55,6 +55,24 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->local_kb_explicit = getenv("ODP_GB300_LOCAL_KB") != NULL;
   t->reorder = env_int("ODP_GB300_REORDER", 1);
   t->direct = env_int("ODP_GB300_DIRECT", 1);
+  t->small_n = env_int("ODP_GB300_SMALL_N", 2048);
+}
+
+/* Chunk width (log2 words) for a graph whose whole level runs in one CTA's
+ * shared memory: the widest of at most 16 words, and at most the graph's own
+ * width, whose two bitset buffers and neighbour table fit; 0 if none does. */
+static int small_wc_log2(int n, int dp, int full_l2)
+{
+  for(int wl = full_l2 < 4 ? full_l2 : 4; wl >= 1; wl--){
+    size_t bytes = 2 * (size_t)n * ((size_t)8 << wl) + (size_t)n * dp * 4;
+    if(bytes <= GBX_SMALL_SMEM_MAX) return wl;
+  }
+  return 0;
+}
+
+static size_t small_bytes(int n, int dp, int wl)
+{
+  return 2 * (size_t)n * ((size_t)8 << wl) + (size_t)n * dp * 4;
 }
 
 static int ilog2_ceil(long long x)
@@ -273,6 +291,26 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   const double budget = (double)tuning->l2_budget_mb * 1024.0 * 1024.0;
   const double local_bytes = (double)tuning->local_kb * 1024.0;
 
+  /* A small plan: every graph has at most small_n vertices and one level of
+   * it (both bitset buffers and the neighbour table) fits in one CTA's shared
+   * memory, so each job runs alone in the small-graph kernel, with no
+   * device-wide hand-off per level.  Mixed plans keep every job in the
+   * persistent engine, whose short jobs fill the end of a run.  Explicit
+   * schedule settings (chunk width, slots, tile rows, one-CTA threshold, a
+   * chunk width from the tuning table) and change tracking select the engine. */
+  int small = count > 0 && tuning->small_n > 0 && tuning->wc_log2 == 0 && tuning->slots == 0 &&
+              tuning->tile_rows == 0 && !tuning->local_kb_explicit;
+  for(int i = 0; i < count && small; i++){
+    const odp_shape *sh = &shapes[i];
+    const int n = sh->grid ? sh->width * sh->height : sh->nodes;
+    const int dp = ALIGN_UP(sh->degree > 0 ? sh->degree : 1, 4);
+    const int W = (n / sh->symmetries + 63) / 64;
+    const ODPX_Tune_entry *te = table_lookup(n, sh->degree, sh->grid);
+    if(n > tuning->small_n || (te && te->wc_log2 > 0) || tracks_changes(tuning, count, sh->grid, n, sh->symmetries) ||
+       !small_wc_log2(n, dp, ilog2_ceil(W < 2 ? 2 : W)))
+      small = 0;
+  }
+
   /* Shapes, chunk widths, tiles. */
   int njobs = 0;
   for(int i = 0; i < count; i++){
@@ -307,6 +345,11 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     if(wl < 1) wl = 1;
     if(wl > 7) wl = 7;                 /* rows of at most 1 KB per chunk */
     if(wl > full_l2 && full_l2 >= 1) wl = full_l2;
+    if(small){
+      wl = small_wc_log2(g->n, g->dp, full_l2);
+      size_t b = small_bytes(g->n, g->dp, wl);
+      if(b > p->small_smem) p->small_smem = b;
+    }
     g->wc_log2 = wl;
     const int wc = 1 << wl;
     g->nchunks = (g->W + wc - 1) / wc;
@@ -323,6 +366,8 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     njobs += g->nchunks;
   }
   p->njobs = njobs;
+  p->small = small;
+  if(small && gbx_small_prepare()){ odp_plan_destroy(p); return ODPX_ERR_CUDA; }
 
   /* Tiles: about 640 KB of traffic each, measured best on GB300 for large
    * single graphs and for most size buckets of the batch.  A plan with few
@@ -548,6 +593,9 @@ static int enqueue(odp_plan *p)
 
 int odp_plan_enqueue_engine(odp_plan *p)
 {
+  if(p->small)
+    return gbx_small_launch(p->d_jobs, p->njobs, (gbx_graph_acc *)(p->d_state + p->acc_off),
+                            (gbx_job_out *)(p->d_state + p->levels_off), p->small_smem, p->stream);
   return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
                            (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),
                            (gbx_job_out *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->any_active,
@@ -685,7 +733,7 @@ int odp_plan_finish(odp_plan *p, odp_result *results)
   unsigned int err = *(const unsigned int *)(p->h_state_out + sizeof(gbx_ctrl)) | ctrl->error;
   if(err & GBX_ERR_TIMEOUT) return ODPX_ERR_TIMEOUT;
   if(err & GBX_ERR_BAD_ADJ) return ODPX_ERR_ADJACENCY;
-  if(p->tuning.reorder && !p->reordered && p->njobs > p->nslots){
+  if(p->tuning.reorder && !p->small && !p->reordered && p->njobs > p->nslots){
     p->reordered = 1;
     int e = reorder_by_duration(p);
     if(e) return e;

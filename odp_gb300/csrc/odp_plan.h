@@ -32,6 +32,7 @@ typedef struct {
   int local_kb_explicit;       /* local_kb was set by the caller: the tuning table does not override it */
   int reorder;                 /* after the first run, order jobs by their measured duration (1, default) */
   int direct;                  /* pull callers' adjacency from host memory when the device can (1, default) */
+  int small_n;                 /* graphs of at most this many vertices may run in shared memory (0: never) */
 } odp_tuning;
 
 typedef struct {
@@ -71,6 +72,8 @@ typedef struct odp_plan {
   int reordered;               /* the job order was learned from a run */
   int direct;                  /* the device pulls the callers' arrays (h_expand holds their pointers) */
   gbx_expand_desc *h_expand;   /* pinned copy of the expand descriptors (direct plans) */
+  int small;                   /* every job runs in the small-graph kernel, in shared memory */
+  size_t small_smem;           /* shared memory per CTA of the small-graph kernel */
 } odp_plan;
 
 typedef struct {

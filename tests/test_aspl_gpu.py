@@ -208,6 +208,41 @@ def test_saturated_lanes_skip_only_what_cannot_change(wc_log2):
         assert same(x, y), (k, x, y)
 
 
+@pytest.mark.parametrize("small_n", ["2048", "0"])
+def test_small_graph_kernel_and_engine_agree(small_n, monkeypatch):
+    """Plans whose graphs all have at most 2048 vertices run every job in
+    the small-graph kernel (bitsets and neighbour table in shared memory);
+    ODP_GB300_SMALL_N=0 sends them through the persistent engine.  Both give
+    the oracle's results, singly and as one batch."""
+    monkeypatch.setenv("ODP_GB300_SMALL_N", small_n)
+    g = lambda n, d, s=1, seed=1: og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, s, seed=seed), d, s)
+    cases = _saturation_cases()                                           # general, s = 4, irregular, disconnected, grid
+    cases.append(og.GraphSpec(g(2048, 12, seed=11), nodes=2048))         # fits with 2-word chunks only
+    cases.append(og.GraphSpec(g(16, 3, seed=12), nodes=16))
+    for s_, w in ((2, 20), (4, 20)):
+        e = og.generate_random_grid(w, w, 4, 3, s_, seed=13)
+        cases.append(og.GraphSpec(og.conv_edge2adjacency_grid(w, w, e, 4, s_), grid=True, width=w, height=w,
+                                  symmetries=s_))
+    refs = [oracle.aspl(c.adjacency, nodes=c.nodes, num_degrees=c.num_degrees, symmetries=c.symmetries,
+                        grid=c.grid, width=c.width, height=c.height) for c in cases]
+    kernel = "engine" if small_n == "0" else "small"
+    b = og.Batch(cases)
+    assert b.kernel() == kernel
+    got = b.run()
+    b.close()
+    for k, (x, y) in enumerate(zip(got, refs)):
+        assert same(x, y), (k, x, y)
+    for c, y in zip(cases, refs):
+        b = og.Batch([c])
+        assert b.kernel() == kernel
+        assert same(b.run()[0], y)
+        b.close()
+    big = og.GraphSpec(g(4096, 8, seed=14), nodes=4096)                 # one graph too large mixes in: engine
+    b = og.Batch(cases[:2] + [big])
+    assert b.kernel() == "engine"
+    b.close()
+
+
 def test_config1_default_kind_and_saving():
     n, d = 1024, 8
     adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=1), d)
