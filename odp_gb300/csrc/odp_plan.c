@@ -300,15 +300,35 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
    * chunk width from the tuning table) and change tracking select the engine. */
   int small = count > 0 && tuning->small_n > 0 && tuning->wc_log2 == 0 && tuning->slots == 0 &&
               tuning->tile_rows == 0 && !tuning->local_kb_explicit;
+  int *small_wl = calloc((size_t)count, sizeof(int));
+  long long small_jobs = 0;
   for(int i = 0; i < count && small; i++){
     const odp_shape *sh = &shapes[i];
     const int n = sh->grid ? sh->width * sh->height : sh->nodes;
     const int dp = ALIGN_UP(sh->degree > 0 ? sh->degree : 1, 4);
     const int W = (n / sh->symmetries + 63) / 64;
     const ODPX_Tune_entry *te = table_lookup(n, sh->degree, sh->grid);
+    small_wl[i] = small_wc_log2(n, dp, ilog2_ceil(W < 2 ? 2 : W));
     if(n > tuning->small_n || (te && te->wc_log2 > 0) || tracks_changes(tuning, count, sh->grid, n, sh->symmetries) ||
-       !small_wc_log2(n, dp, ilog2_ceil(W < 2 ? 2 : W)))
+       !small_wl[i])
       small = 0;
+    small_jobs += (W + (1 << small_wl[i]) - 1) >> small_wl[i];
+  }
+  /* Each job takes one SM: narrower chunks give a plan with few jobs more of
+   * them (the n = 1024, d = 8 graph: 2 jobs of 8 words, or 8 of 2 words, each
+   * gathering a quarter of the bytes), until the jobs cover the SMs. */
+  if(small){
+    const int sms = gbx_engine_blocks(0) / 4 > 0 ? gbx_engine_blocks(0) / 4 : 1;
+    while(small_jobs < sms){
+      int k = -1;
+      for(int i = 0; i < count; i++)
+        if(small_wl[i] > 1 && (k < 0 || small_wl[i] > small_wl[k])) k = i;
+      if(k < 0) break;
+      const int n = shapes[k].grid ? shapes[k].width * shapes[k].height : shapes[k].nodes;
+      const int W = (n / shapes[k].symmetries + 63) / 64;
+      small_jobs += ((W + (1 << (small_wl[k] - 1)) - 1) >> (small_wl[k] - 1)) - ((W + (1 << small_wl[k]) - 1) >> small_wl[k]);
+      small_wl[k]--;
+    }
   }
 
   /* Shapes, chunk widths, tiles. */
@@ -346,7 +366,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     if(wl > 7) wl = 7;                 /* rows of at most 1 KB per chunk */
     if(wl > full_l2 && full_l2 >= 1) wl = full_l2;
     if(small){
-      wl = small_wc_log2(g->n, g->dp, full_l2);
+      wl = small_wl[i];
       size_t b = small_bytes(g->n, g->dp, wl);
       if(b > p->small_smem) p->small_smem = b;
     }
@@ -367,6 +387,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   }
   p->njobs = njobs;
   p->small = small;
+  free(small_wl);
   if(small && gbx_small_prepare()){ odp_plan_destroy(p); return ODPX_ERR_CUDA; }
 
   /* Tiles: about 640 KB of traffic each, measured best on GB300 for large
