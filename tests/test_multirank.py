@@ -60,3 +60,28 @@ def test_dist_helper_takes_the_max_over_ranks(tmp_path):
     rec = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][0])
     assert rec["max_ms"] == 15.0
     assert abs(rec["value"] - 2 * 100 * 1000.0 / 15.0) < 1e-9
+
+
+def test_reference_arm_json_line_carries_the_contract_keys():
+    """One process: the reference arm's line has the keys of the bench
+    contract, its cpu_baseline describes this run, and its e2e moves no
+    bytes (the work runs on the host)."""
+    cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--graphs", "12", "--steps", "2",
+           "--warmup", "3", "--cpu-seconds", "0.5"]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=280, cwd=ROOT)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1, r.stdout
+    rec = json.loads(lines[0])
+    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better", "scaling",
+              "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"):
+        assert k in rec, k
+    assert rec["impl"] == "reference" and rec["steps"] == 2 and rec["warmup"] == 3 and rec["n_gpus"] == 1
+    assert rec["higher_is_better"] is True and rec["value"] > 0 and rec["ms_per_step"] > 0
+    assert "workload" in rec["config"]
+    cb = rec["cpu_baseline"]
+    assert cb["value"] == rec["value"] and cb["unit"] == rec["unit"] and cb["cores"] >= 1
+    assert cb["kind"] in ("reference", "port") and cb["sample"]
+    e = rec["e2e"]
+    assert e["value"] == rec["value"] and e["unit"] == rec["unit"]
+    assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
