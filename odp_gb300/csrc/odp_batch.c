@@ -238,11 +238,15 @@ int ODPX_Batch_job_profile(const ODPX_Batch *batch, int *graph, double *loaded_u
   if(!batch) return ODPX_ERR_STATE;
   const gbx_job_out *jo = odp_plan_job_out(batch);
   int n = batch->njobs < max_jobs ? batch->njobs : max_jobs;
+  /* time origin: the engine's start, or the earliest stamp (the small-graph
+   * kernel does not set the engine's) */
   unsigned long long t0 = ((const gbx_ctrl *)batch->h_state_out)->t_start;
+  if(t0 == 0) t0 = ~0ull;
   for(int i = 0; i < batch->njobs; i++){
     if(jo[i].t_loaded && jo[i].t_loaded < t0) t0 = jo[i].t_loaded;
     if(jo[i].t_done && jo[i].t_done < t0) t0 = jo[i].t_done;
   }
+  if(t0 == ~0ull) t0 = 0;
   for(int i = 0; i < n; i++){
     if(graph) graph[i] = batch->h_jobs[i].graph;
     loaded_us[i] = jo[i].t_loaded ? (double)(jo[i].t_loaded - t0) * 1e-3 : 0.0;
