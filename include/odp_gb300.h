@@ -70,8 +70,9 @@ unsigned long long ODPX_Batch_tiles(const ODPX_Batch *batch);
 /* Introspection for benchmarks: jobs, slots, chunk width (log2 words) of graph i. */
 int  ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots, int *wc_log2, int *tile_rows);
 /* Which kernel evaluates the plan: 1 when every graph has at most
- * ODP_GB300_SMALL_N (default 2048) vertices and one level of each fits in
- * one CTA's shared memory, so each job runs alone in the small-graph kernel;
+ * ODP_GB300_SMALL_N (default 2048) vertices, one level of each fits in one
+ * CTA's shared memory and the plan has at most one job per SM, so each job
+ * runs alone in the small-graph kernel;
  * 0 for the persistent engine (mixed plans, explicit schedule settings,
  * change tracking).  Results are the same either way. */
 int  ODPX_Batch_kernel(const ODPX_Batch *batch);

@@ -314,11 +314,15 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       small = 0;
     small_jobs += (W + (1 << small_wl[i]) - 1) >> small_wl[i];
   }
-  /* Each job takes one SM: narrower chunks give a plan with few jobs more of
-   * them (the n = 1024, d = 8 graph: 2 jobs of 8 words, or 8 of 2 words, each
-   * gathering a quarter of the bytes), until the jobs cover the SMs. */
+  /* Each job takes one SM.  A plan with more jobs than SMs stays on the
+   * engine, which keeps four CTAs per SM busy with them (the small kernel is
+   * measured on single graphs and small groups only).  Narrower chunks give a
+   * plan with few jobs more of them (the n = 1024, d = 8 graph: 2 jobs of 8
+   * words, or 8 of 2 words, each gathering a quarter of the bytes), until the
+   * jobs cover the SMs. */
+  const int sms = gbx_engine_blocks(0) / 4 > 0 ? gbx_engine_blocks(0) / 4 : 1;
+  if(small && small_jobs > sms) small = 0;
   if(small){
-    const int sms = gbx_engine_blocks(0) / 4 > 0 ? gbx_engine_blocks(0) / 4 : 1;
     while(small_jobs < sms){
       int k = -1;
       for(int i = 0; i < count; i++)
