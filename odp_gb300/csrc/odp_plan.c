@@ -276,11 +276,11 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   int rc = 0;
   *out = NULL;
   if(count <= 0) return ODPX_ERR_INVALID;
-  if(odp_device_ready()) return ODPX_ERR_CUDA;
-  for(int i = 0; i < count; i++){
+  for(int i = 0; i < count; i++){          /* arguments first: refused the same with or without a device */
     rc = validate_shape(&shapes[i]);
     if(rc) return rc;
   }
+  if(odp_device_ready()) return ODPX_ERR_CUDA;
 
   odp_plan *p = calloc(1, sizeof(odp_plan));
   p->tuning = *tuning;

@@ -34,3 +34,22 @@ def test_library_exports_every_declared_symbol():
 def test_static_archive_built():
     import odp_gb300.build as b
     assert os.path.exists(b.A_PATH)
+
+
+def test_invalid_batch_shapes_are_refused_before_the_device():
+    """Shapes are validated before any device work, so they are refused with
+    ODPX_ERR_INVALID on any machine: nodes not a multiple of the symmetries,
+    a grid with s = 2 and an odd width, a grid with s = 4 that is not square."""
+    import numpy as np
+    import odp_gb300 as og
+    cases = [dict(nodes=10, symmetries=3), dict(grid=True, width=5, height=6, symmetries=2),
+             dict(grid=True, width=6, height=8, symmetries=4)]
+    for kw in cases:
+        n = kw.get("nodes") or kw["width"] * kw["height"]
+        adj = np.zeros((max(1, n // kw["symmetries"]), 4), dtype=np.int32)
+        try:
+            og.Batch([og.GraphSpec(adj, **kw)])
+        except og.ODPError as e:
+            assert e.code == og.ERR_INVALID, (kw, e.code)
+        else:
+            raise AssertionError("accepted: %s" % kw)
