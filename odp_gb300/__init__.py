@@ -78,6 +78,8 @@ def load():
         "ODP_Conv_edge2adjacency_general_s": (None, [I, I, I, P, I, P]),
         "ODP_Conv_edge2adjacency_grid": (None, [I, I, I, I, P, P]),
         "ODP_Conv_edge2adjacency_grid_s": (None, [I, I, I, I, P, I, P]),
+        "ODP_Set_lbounds_general": (None, [I, I, IP, ctypes.POINTER(ctypes.c_double)]),
+        "ODP_Set_lbounds_grid": (None, [I, I, I, I, IP, ctypes.POINTER(ctypes.c_double)]),
         "ODP_Conv_adjacency2edge_general": (None, [I, I, P, P, P]),
         "ODP_Conv_adjacency2edge_general_s": (None, [I, I, P, P, I, P]),
         "ODP_Conv_adjacency2edge_grid": (None, [I, I, I, P, P, P]),
@@ -238,6 +240,20 @@ def conv_edge2adjacency_general(nodes, edge, degree, symmetries=1):
     adj = np.zeros((nodes // symmetries, degree), dtype=np.int32)
     load().ODP_Conv_edge2adjacency_general_s(nodes, len(edge), degree, _iptr(edge), symmetries, _iptr(adj))
     return adj
+
+
+def set_lbounds_general(nodes, degree):
+    """ODP_Set_lbounds_general: (low_diameter, low_ASPL), the Moore bound."""
+    d, a = ctypes.c_int(), ctypes.c_double()
+    load().ODP_Set_lbounds_general(nodes, degree, ctypes.byref(d), ctypes.byref(a))
+    return d.value, a.value
+
+
+def set_lbounds_grid(width, height, degree, length):
+    """ODP_Set_lbounds_grid: (low_diameter, low_ASPL), the lattice bound."""
+    d, a = ctypes.c_int(), ctypes.c_double()
+    load().ODP_Set_lbounds_grid(width, height, degree, length, ctypes.byref(d), ctypes.byref(a))
+    return d.value, a.value
 
 
 def get_lines(fname):

@@ -10,6 +10,8 @@
 #include <stdlib.h>
 #include <stdbool.h>
 #include <math.h>
+#include <limits.h>
+#include <float.h>
 #include <string.h>
 #include <pthread.h>
 #include <unistd.h>
@@ -20,60 +22,129 @@
 static int max_i(int a, int b) { return a > b ? a : b; }
 static int min_i(int a, int b) { return a < b ? a : b; }
 
-/* ODP_Set_lbounds_general, utils.c:1431-1459: the Moore bound. */
-void ODP_Set_lbounds_general(int nodes, int degree, int *low_diameter, double *low_ASPL)
+/* ---------------------------------------------------------------------- */
+/* Lower bounds printed as the "gap" lines of the sample programs.          */
+/* ---------------------------------------------------------------------- */
+
+/* Vertices that a graph of maximum degree d can hold within k hops of one
+ * vertex (the Moore bound): 1 + d + d(d-1) + ... + d(d-1)^(k-1), clamped to
+ * `cap`. */
+static long long moore_ball(int degree, int k, long long cap)
 {
-  int diam = -1, n = 1, r = 1;
-  double aspl = 0.0;
-  for(;;){
-    int reach = n + degree * pow(degree - 1, r - 1);
-    if(reach >= nodes) break;
-    n = reach;
-    aspl += r * degree * pow(degree - 1, r - 1);
-    diam = r++;
+  long long ball = 1, shell = degree;
+  for(int r = 1; r <= k && ball < cap; r++){
+    ball += shell;
+    if(shell > cap) shell = cap;        /* no overflow; the ball is clamped anyway */
+    else shell *= degree - 1;
   }
-  diam++;
-  aspl += diam * (nodes - n);
-  aspl /= (nodes - 1);
-  *low_diameter = diam;
-  *low_ASPL = aspl;
+  return ball < cap ? ball : cap;
 }
 
-/* ODP_Set_lbounds_grid, utils.c:1461-1504: per-vertex hop histogram capped
- * by the Moore bound, with edges of at most `length` lattice steps. */
+/* ODP_Set_lbounds_general (reference utils.c:1431-1459): the Moore bound for
+ * `nodes` vertices of degree `degree`.  Distances from one vertex fill shells
+ * r = 1, 2, ... of at most d(d-1)^(r-1) vertices each; the bound puts every
+ * vertex in the nearest shell with room.  The ASPL bound is the mean distance
+ * of that arrangement, the diameter bound its last shell.  The sum is an
+ * integer, so one division gives the double the reference computes.  When
+ * one hop already reaches every vertex (nodes <= degree + 1) the reference
+ * reports diameter 0 and ASPL 0.0, and so does this function; a degree that
+ * can never reach every vertex (d < 2 with more than d + 1 vertices) has no
+ * finite bound: INT_MAX and DBL_MAX, where the reference does not return. */
+void ODP_Set_lbounds_general(int nodes, int degree, int *low_diameter, double *low_ASPL)
+{
+  if(nodes <= degree + 1){
+    *low_diameter = 0;
+    *low_ASPL = 0.0;
+    return;
+  }
+  long long placed = 1, distance_sum = 0, shell = degree;
+  int r = 1;
+  for(;;){
+    const long long left = (long long)nodes - placed;
+    if(shell >= left){
+      distance_sum += (long long)r * left;
+      break;
+    }
+    if(shell <= 0){
+      *low_diameter = INT_MAX;
+      *low_ASPL = DBL_MAX;
+      return;
+    }
+    distance_sum += (long long)r * shell;
+    placed += shell;
+    shell *= degree - 1;
+    r++;
+  }
+  *low_diameter = r;
+  *low_ASPL = (double)distance_sum / (double)(nodes - 1);
+}
+
+/* Lattice points of an m x n grid within Manhattan distance D of (i, j):
+ * for every row offset a, the rows at that offset (one or two) times the
+ * columns within D - a. */
+static long long lattice_ball(int m, int n, int i, int j, long long D)
+{
+  const int up = i, down = m - 1 - i, left = j, right = n - 1 - j;
+  const long long amax = D < (up > down ? up : down) ? D : (up > down ? up : down);
+  long long count = 0;
+  for(long long a = 0; a <= amax; a++){
+    const long long rows = a == 0 ? 1 : (a <= up) + (a <= down);
+    const long long x = D - a;
+    const long long cols = 1 + (x < left ? x : left) + (x < right ? x : right);
+    count += rows * cols;
+  }
+  return count;
+}
+
+/* ODP_Set_lbounds_grid (reference utils.c:1461-1504, after the graph-golf
+ * lattice bound): on an m x n grid whose edges span at most `length` lattice
+ * steps, a vertex at Manhattan distance D from v is at least ceil(D / length)
+ * hops away, and no more than the Moore ball of k hops is within k hops.  So
+ * at most B_v(k) = min(#lattice points within k * length of v, Moore(k))
+ * vertices lie within k hops of v, and the distances from v sum to at least
+ * sum over k >= 0 of (mn - B_v(k)).  The ASPL bound averages that over all
+ * ordered pairs; the diameter bound is the least k with B_v(k) = mn at a
+ * corner vertex (a corner is farthest from everything, as in the
+ * reference, which reads it from its last vertex, (m-1, n-1)).  Reflections
+ * of the grid keep B_v, so one quadrant of vertices is enough; the integer
+ * sum gives the reference's double after one division. */
 void ODP_Set_lbounds_grid(int m, int n, int degree, int length, int *low_diameter, double *low_ASPL)
 {
-  int mn = m * n, current = degree, ii;
-  int cap = mn + m + n + 8;
-  int *moore = calloc((size_t)cap, sizeof(int));
-  int *hist = calloc((size_t)cap, sizeof(int));
-  int *mh = calloc((size_t)cap, sizeof(int));
-  double sum = 0;
-  moore[0] = 1;
-  moore[1] = degree + 1;
-  for(ii = 2;; ii++){
-    current = current * (degree - 1);
-    moore[ii] = moore[ii - 1] + current;
-    if(moore[ii] >= mn){ moore[ii] = mn; break; }
+  const long long mn = (long long)m * n;
+  if(degree < 2 && mn > degree + 1){           /* the Moore ball never covers the grid */
+    *low_diameter = INT_MAX;
+    *low_ASPL = DBL_MAX;
+    return;
   }
-  int maxhop = max_i((m + n - 2 + (length - 1)) / length, ii);
-  for(int i = ii + 1; i <= maxhop; i++) moore[i] = mn;
-  for(int i = 0; i < m; i++){
-    for(int j = 0; j < n; j++){
-      for(int k = 0; k <= maxhop; k++) hist[k] = 0;
-      for(int i2 = 0; i2 < m; i2++)
-        for(int j2 = 0; j2 < n; j2++)
-          hist[(abs(i - i2) + abs(j - j2) + length - 1) / length]++;
-      for(int k = 1; k <= maxhop; k++) hist[k] += hist[k - 1];
-      for(int k = 0; k <= maxhop; k++) mh[k] = min_i(hist[k], moore[k]);
-      for(int k = 1; k <= maxhop; k++) sum += (double)(mh[k] - mh[k - 1]) * k;
+  const long long span = (long long)(m - 1) + (n - 1);            /* largest Manhattan distance */
+  int kmax = (int)((span + length - 1) / length);
+  while(moore_ball(degree, kmax, mn) < mn) kmax++;                /* both parts of B reach mn by kmax */
+  long long *moore = malloc(sizeof(long long) * (size_t)(kmax + 1));
+  for(int k = 0; k <= kmax; k++) moore[k] = moore_ball(degree, k, mn);
+
+  long long missing = 0;                       /* sum over v and k of (mn - B_v(k)) */
+  for(int i = 0; i < (m + 1) / 2; i++){
+    const int mult_i = (2 * i + 1 == m) ? 1 : 2;
+    for(int j = 0; j < (n + 1) / 2; j++){
+      const int mult_j = (2 * j + 1 == n) ? 1 : 2;
+      long long v = 0;
+      for(int k = 0; k < kmax; k++){
+        long long b = lattice_ball(m, n, i, j, (long long)k * length);
+        if(b > moore[k]) b = moore[k];
+        if(b == mn) break;
+        v += mn - b;
+      }
+      missing += v * mult_i * mult_j;
     }
   }
-  int dboth = 0;
-  while(mh[dboth] != mn) dboth++;
-  *low_diameter = dboth;
-  *low_ASPL = sum / ((double)mn * (mn - 1));
-  free(moore); free(hist); free(mh);
+  int diam = 0;
+  for(;; diam++){
+    long long b = lattice_ball(m, n, m - 1, n - 1, (long long)diam * length);
+    if((b < moore[diam] ? b : moore[diam]) == mn) break;
+  }
+  free(moore);
+  *low_diameter = diam;
+  *low_ASPL = (double)missing / ((double)mn * (double)(mn - 1));
 }
 
 /* ODP_Set_degrees, utils.c:1545-1555 */

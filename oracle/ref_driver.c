@@ -20,6 +20,9 @@
  *   mutate grid   W H D LEN S SEED ITERS ADJ OUT  ODP_Mutate_adjacency_grid_s trace
  *   lines FILE                          ODP_Get_lines (edge text files)
  *   readedges general|grid FILE OUT     ODP_Read_edge_* -> raw pairs
+ *   lbounds general N D                 ODP_Set_lbounds_general
+ *   lbounds grid W H D LEN              ODP_Set_lbounds_grid
+ *                                       ("<diameter> <ASPL as %a>")
  *
  * "aspl" prints one line: "<diameter> <sum> <ASPL as %a hex float> <ASPL %.10f>".
  * "mutate" writes, per iteration, the 8 ints of ODP_Restore followed by the
@@ -185,6 +188,14 @@ int main(int argc, char **argv)
       printf("%d %d %d\n", lines, w, h);
     }
     write_file(argv[4], edge, sizeof(int) * 2 * (size_t)lines);
+    return 0;
+  }
+
+  if(strcmp(cmd, "lbounds") == 0){
+    int low_diameter; double low_aspl;
+    if(!grid) ODP_Set_lbounds_general(atoi(argv[3]), atoi(argv[4]), &low_diameter, &low_aspl);
+    else      ODP_Set_lbounds_grid(atoi(argv[3]), atoi(argv[4]), atoi(argv[5]), atoi(argv[6]), &low_diameter, &low_aspl);
+    printf("%d %a\n", low_diameter, low_aspl);
     return 0;
   }
 

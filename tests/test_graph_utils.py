@@ -7,6 +7,7 @@ import numpy as np
 import pytest
 
 import odp_gb300 as og
+import oracle
 from conftest import gen_record_adjacency, gen_record_edges, sha256
 
 
@@ -121,3 +122,25 @@ def test_restore_before_any_mutate_is_refused():
     """ % ROOT)
     r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=60)
     assert r.returncode == 1 and "before ODP_Mutate" in r.stderr
+
+
+@pytest.mark.skipif(oracle.ref_driver() is None, reason="reference library not built")
+def test_lower_bounds_match_reference():
+    """ODP_Set_lbounds_general / _grid (the "gap" lines of the sample
+    programs) give the reference's diameter and ASPL bits."""
+    import subprocess
+    drv = oracle.ref_driver()
+
+    def ref(*args):
+        out = subprocess.run([drv, "lbounds"] + [str(a) for a in args], capture_output=True, text=True,
+                             timeout=60, check=True).stdout.split()
+        return int(out[0]), float.fromhex(out[1])
+
+    for n in (4, 5, 10, 12, 16, 17, 72, 100, 256, 1000, 65536, 10 ** 6):
+        for d in (2, 3, 4, 6, 10, 16, 32):
+            r, g = ref("general", n, d), og.set_lbounds_general(n, d)
+            assert r[0] == g[0] and r[1].hex() == g[1].hex(), (n, d, r, g)
+    for m, n, d, length in [(4, 4, 3, 2), (5, 5, 4, 2), (6, 6, 3, 2), (4, 6, 3, 2), (7, 9, 4, 3), (12, 12, 5, 3),
+                            (20, 12, 6, 4), (30, 30, 8, 3), (40, 20, 8, 5), (64, 64, 4, 3), (90, 90, 32, 3)]:
+        r, g = ref("grid", m, n, d, length), og.set_lbounds_grid(m, n, d, length)
+        assert r[0] == g[0] and r[1].hex() == g[1].hex(), (m, n, d, length, r, g)
