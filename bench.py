@@ -11,26 +11,35 @@ Reported on rank 0 as one JSON line:
                CUDA events on the plan's stream, L2 flushed before each run)
   e2e          batched evals/s through ODP_Set_aspl_batch with the adjacency in
                host memory (upload, expand, engine, read back, decode)
-  per_call     evals/s of the one-graph-per-call path on the same GPU: a plan
-               per graph evaluated one after the other (the fastest per-call
-               form), and the drop-in Init/Set/Finalize cycle
-  single_graph the n=65536, d=16 graph of the reference's MATRIX_SAVING
-               configuration: device and ODP_Set_aspl evals/s
-  roofline     algorithmic bytes of the engine kernel per launch / its time,
-               against the measured HBM peak; the measured L2 read ceiling
-               is reported beside it (the working set is L2-resident)
+  per_call     evals/s of one graph per call on the same GPU over the same 512
+               graphs: a plan per graph (ODPX_Batch_run), the drop-in
+               Init/Set/Finalize cycle, and the reference's own libodp_cuda.a
+               rebuilt for sm_103a (ODP_Set_aspl per graph, in its own process)
+  configs      the reference's configurations one graph at a time: n=1024 d=8;
+               n=65536 d=16 (MATRIX_SAVING); n=262144 d=24 s=64; the 256x256
+               grid.  Device time, ODP_Set_aspl end to end, bytes, the
+               roofline fraction, and the reference's CPU (libodp_threads.a)
+               and GPU (libodp_cuda.a) times for the same graph
+  single_graph the n=65536, d=16 graph, autotuned
+  roofline     the batched engine kernel against the L2 read ceiling (its
+               bitsets are L2-resident): bytes actually read from L2 per second
+               over the ceiling measured live by a streaming probe; the
+               algorithmic bytes, the DRAM traffic and the HBM peak beside it
   serving      64 simulated-annealing chains (n in {1024..32768}, d in {8,16,24})
                proposing 2-opt swaps to the serving mode (ODPX_Serve_*): closed
                loop, one request outstanding per chain, exponential think time
-               for a 20k req/s offered cap; evals/s and p50/p99 latency, beside
-               the same proposals evaluated one call at a time
+               for a 20k req/s offered cap; p50/p99 latency, results checked
+               against each graph evaluated alone; a saturating run of the
+               n <= 8192 chains; per-call evals/s of the same request mix
   anneal       the same 64 chains with every step (2-opt proposal, evaluation,
                acceptance, undo) on the GPU (ODPX_Anneal), in 4 size groups
-  cpu_baseline the oracle port of the reference CPU library (OpenMP, all host
-               cores) on a bounded sample of the batch
+  cpu_baseline the reference's libodp_threads.a (OpenMP, all host cores) on
+               the batch
 
---impl reference times the reference's CPU implementation (the oracle port,
-all host threads) on the same batch and prints the same line shape.
+--impl reference times the reference's CPU library libodp_threads.a, built
+from its own sources (baseline/), on the same 512 graphs, which it generates
+with the reference's own generators; that process loads nothing of
+libodp_gb300.
 """
 import argparse
 import hashlib
@@ -48,17 +57,22 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "ASPL evals/s, batched vs per-call on 1 GB300 (bit-exact)"
-C2 = dict(nodes=65536, degree=16, seed=2, sha256="d855fb662f9e9557", result=(6, 9346294313))
 WORKLOAD = ("batched: 512 graphs, seeds 100..611, n log-uniform [256, 8192], d in {4..32}, "
             "80% general / 20% grid (length 3-6), s in {1,2,4}")
-# One ncu capture of an engine_kernel launch on the first 128 graphs of the batch
-# (profiles/engine_kernel_batch.md): DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum), bytes
-# read from L2 by the SMs (l1tex__m_xbar2l1tex_read_bytes.sum), and that launch's algorithmic bytes.  A full
-# batch launch's figures are taken as these scaled by algorithmic bytes.  The engine reads fewer bytes than
-# the algorithmic count: level 1 is built from the neighbour lists, and lanes whose words are saturated
-# gather nothing.
-NCU_DRAM = {"bytes": 936275200.0 + 815841024.0, "l2_read_bytes": 14874844864.0, "bytes_alg": 24803482864.0,
-            "graphs": 128}
+L2_NOTE = "GPU arm: L2 flushed (512 MB write) before every timed device run"
+# sha256 over the 512 adjacency arrays of the batch, concatenated in order: the
+# same for the reference generators (baseline/ref_bench.c gen) and the
+# library's own; both arms check it, so they evaluate identical graphs.
+BATCH_SHA256 = "cb594241cefc45d1"
+# ncu counters of one engine_kernel launch at this build and schedule, per
+# algorithmic byte of the same launch (ncu --metrics dram__bytes_read.sum,
+# dram__bytes_write.sum, l1tex__m_xbar2l1tex_read_bytes.sum; bytes_alg from
+# ODPX_Batch_bytes_alg): "batch" on the first 128 graphs of the batch, "C2"..
+# on the configuration graphs.  A launch's L2 read bytes and DRAM traffic are
+# taken as its algorithmic bytes times these ratios.
+NCU_RATIOS = {
+    "batch": {"l2_read": 14874844864.0 / 24803482864.0, "dram": (936275200.0 + 815841024.0) / 24803482864.0},
+}
 
 
 def parse():
@@ -72,7 +86,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-single", action="store_true")
     p.add_argument("--no-per-call", action="store_true")
-    p.add_argument("--cpu-seconds", type=float, default=10.0)
+    p.add_argument("--no-configs", action="store_true")
+    p.add_argument("--no-reference-gpu", action="store_true")
     p.add_argument("--no-serving", action="store_true")
     p.add_argument("--no-anneal", action="store_true")
     p.add_argument("--no-tune", action="store_true")
@@ -170,22 +185,204 @@ def measured_peaks():
         return {"hbm_gbs": 6800.0}, "fallback"
 
 
+def same(a, b):
+    return a[0] == b[0] and a[1] == b[1] and float(a[2]).hex() == float(b[2]).hex()
+
+
+def adjacency_sha(adjs):
+    h = hashlib.sha256()
+    for a in adjs:
+        h.update(np.ascontiguousarray(a, dtype="<i4").tobytes())
+    return h.hexdigest()[:16]
+
+
+def common_config(count):
+    """The `config` of both arms (identical keys and values)."""
+    return {"workload": WORKLOAD, "graphs": count, "l2": L2_NOTE}
+
+
+# ---------------------------------------------------------------------------
+# Reference arm: libodp_threads.a on the host cores.
+# ---------------------------------------------------------------------------
+
+def unavailable(why):
+    print(json.dumps({"impl": "reference", "unavailable": why}))
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    import baseline
+    from odp_gb300 import workloads       # the shape list only; nothing here loads libodp_gb300
+    if not baseline.cpu_available():
+        ok, _ = baseline.build(cpu=True, gpu=False)
+        if not ok:
+            return unavailable("the reference library could not be built from baseline/_ref/src "
+                               "(reference sources %s)" % ("present" if baseline.sources_present() else "absent"))
+    shapes = workloads.batch_shapes(args.graphs)
+    t0 = time.perf_counter()
+    adjs = baseline.generate(shapes)
+    gen_s = time.perf_counter() - t0
+    sha = adjacency_sha(adjs)
+    if args.graphs == 512 and sha != BATCH_SHA256:
+        raise RuntimeError("the reference generators gave other graphs than expected (%s)" % sha)
+    steps, _ = baseline.time_cpu(shapes, adjs, steps=args.steps, warmup=args.warmup, sets=2)
+    total_ns = sum(s["warm_ns"] for s in steps)
+    v = len(shapes) * len(steps) / (total_ns * 1e-9)
+    host = baseline.host_description()
+    sample = ("every step the whole batch: per graph a forked child of libodp_threads.a (Init, an untimed "
+              "ODP_Set_aspl, a timed ODP_Set_aspl, Finalize), OMP_NUM_THREADS=%d; %d graphs over %d steps, "
+              "%.2f s of timed Set calls" % (host["nproc"], len(shapes) * len(steps), len(steps), total_ns * 1e-9))
+    line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ns * 1e-6 / len(steps), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
+            "data": "synthetic (reference generators, seeded)", "impl": "reference",
+            "config": common_config(len(shapes)),
+            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": host["nproc"], "kind": "reference",
+                             "cpu_model": host["cpu_model"], "nproc": host["nproc"], "sample": sample},
+            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "reference": {"library": "libodp_threads.a built from the reference sources (-O3 -march=native "
+                                     "-fopenmp)", "generation_s": gen_s, "adjacency_sha256": sha,
+                          "first_set_evals_per_s": len(shapes) * len(steps) /
+                          (sum(s["first_ns"] for s in steps) * 1e-9)}}
+    line["reference"]["odp_gb300_mapped"] = odp_gb300_mapped()
+    if line["reference"]["odp_gb300_mapped"]:
+        raise RuntimeError("the reference arm mapped a libodp_gb300 library")
+    print(json.dumps(line))
+
+
+def odp_gb300_mapped():
+    """True if this process has any libodp_gb300 library mapped."""
+    try:
+        with open("/proc/self/maps") as f:
+            return any("libodp_gb300" in ln for ln in f)
+    except OSError:
+        return False
+
+
+# ---------------------------------------------------------------------------
+# Own arm.
+# ---------------------------------------------------------------------------
+
 def batch_workload(count):
     from odp_gb300 import workloads
     shapes = workloads.batch_shapes(count)
     return shapes, workloads.build_graphs(shapes)
 
 
-def single_graph():
+def load_golden():
+    with open(os.path.join(ROOT, "tests", "golden", "golden.json")) as f:
+        return json.load(f)
+
+
+def config_graphs():
+    """The reference's four configurations: (name, workload, spec, shape,
+    expected result, env for the reference library)."""
     import odp_gb300 as og
-    e = og.generate_random_general(C2["nodes"], C2["degree"], seed=C2["seed"])
-    if not hashlib.sha256(np.ascontiguousarray(e, dtype=np.int32).tobytes()).hexdigest().startswith(C2["sha256"]):
-        raise RuntimeError("generated n=65536 graph differs from the reference's")
-    return og.conv_edge2adjacency_general(C2["nodes"], e, C2["degree"])
+    gold = {g.get("name") or (g["kind"], g.get("nodes"), g.get("degree"), g.get("seed")): g
+            for g in load_golden()["generators"]}
+
+    def expect(r):
+        return (r[0], r[1], float.fromhex(r[2]))
+
+    out = []
+    for name, key, n, d, s, seed, env in (
+            ("C1", ("general", 1024, 8, 1), 1024, 8, 1, 1, None),
+            ("C2", "single_large_65536", 65536, 16, 1, 2, {"ODP_ASPL": "MATRIX_SAVING"}),
+            ("C3", "symmetric_262144", 262144, 24, 64, 3, None)):
+        g = gold[key]
+        e = og.generate_random_general(n, d, s, seed=seed)
+        if hashlib.sha256(np.ascontiguousarray(e, dtype=np.int32).tobytes()).hexdigest() != g["sha256"]:
+            raise RuntimeError("generated %s graph differs from the reference's" % name)
+        adj = og.conv_edge2adjacency_general(n, e, d, s)
+        out.append(dict(name=name, workload="general n=%d d=%d s=%d seed=%d" % (n, d, s, seed),
+                        spec=og.GraphSpec(adj, nodes=n, symmetries=s),
+                        shape=dict(grid=False, nodes=n, degree=d, symmetries=s, seed=seed),
+                        expected=expect(g["reference"]), env=env))
+    g = gold["grid_256x256"]
+    z = np.load(os.path.join(ROOT, "tests", "golden", "grid_256x256_d6_l4_seed4.npz"))
+    codes = z["codes"].astype(np.int32)
+    w = h = 256
+    v = np.arange(w * h)[:, None]
+    adj = ((v // h + codes // 9 - 4) * h + (v % h + codes % 9 - 4)).astype(np.int32)
+    if hashlib.sha256(adj.tobytes()).hexdigest() != bytes(z["adjacency_sha256"]).decode():
+        raise RuntimeError("256x256 grid fixture damaged")
+    out.append(dict(name="G", workload="grid 256x256 d=6 length 4 seed=4 (diameter 140)",
+                    spec=og.GraphSpec(adj, grid=True, width=w, height=h),
+                    shape=dict(grid=True, width=w, height=h, degree=6, length=4, symmetries=1, seed=4),
+                    expected=expect(g["reference"]), env=None))
+    return out
+
+
+def live_bytes(spec, info):
+    """Bytes of the bitset buffers a plan keeps live (both buffers of every slot)."""
+    n = spec.width * spec.height if spec.grid else spec.nodes
+    return 2.0 * info["nslots"] * n * 8.0 * (1 << info["wc_log2"])
+
+
+def time_configs(args, l2_gbs, hbm_gbs, l2_bytes):
+    import odp_gb300 as og
+    import baseline
+    out = {}
+    reps = {"C1": 200, "C2": 10, "C3": 20, "G": 4}
+    for c in config_graphs():
+        spec, name = c["spec"], c["name"]
+        b = og.Batch([spec])
+        r = b.run()[0]
+        assert same(r, c["expected"]), (name, r, c["expected"])
+        b.time(2, mode=1, flush_mb=args.flush_mb)
+        ms = b.time(reps[name], mode=1, flush_mb=args.flush_mb)
+        balg = b.bytes_alg()
+        info = b.info(0)
+        kernel = b.kernel()
+        b.close()
+        # ODP_Set_aspl end to end: host adjacency, copies and decode included
+        nd = None
+        if spec.grid:
+            og.init_aspl_grid(spec.width, spec.height, spec.degree, nd)
+        elif spec.symmetries == 1:
+            og.init_aspl_general(spec.nodes, spec.degree, nd)
+        else:
+            og.init_aspl_general_s(spec.nodes, spec.degree, nd, spec.symmetries)
+        og.set_aspl(spec.adjacency)
+        k = reps[name]
+        t0 = time.perf_counter()
+        for _ in range(k):
+            r2 = og.set_aspl(spec.adjacency)
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / k
+        og.finalize_aspl()
+        assert same(r2, c["expected"])
+        live = live_bytes(spec, info)
+        rec = {"workload": c["workload"], "kernel": kernel, "device_ms": ms, "set_aspl_e2e_ms": e2e_ms,
+               "bytes_alg": balg, "alg_gbs": balg / (ms * 1e-3) / 1e9, "live_bitset_bytes": live,
+               "bound": "l2" if live <= l2_bytes else "hbm",
+               "result": {"diameter": r[0], "sum": r[1], "ASPL": r[2]}}
+        ratio = NCU_RATIOS.get(name)
+        if ratio:
+            moved = balg * ratio["l2_read"]
+            rec.update({"l2_read_bytes": moved, "l2_read_gbs": moved / (ms * 1e-3) / 1e9,
+                        "l2_read_frac": moved / (ms * 1e-3) / 1e9 / l2_gbs,
+                        "dram_bytes": balg * ratio["dram"],
+                        "dram_frac_of_hbm": balg * ratio["dram"] / (ms * 1e-3) / 1e9 / hbm_gbs})
+        if baseline.cpu_available() and not args.no_cpu_baseline:
+            sets = 1 if name == "G" else 2
+            steps, res = baseline.time_cpu([c["shape"]], [spec.adjacency], steps=1 if name in ("G", "C2", "C3")
+                                           else 20, warmup=0, sets=sets, env=c["env"])
+            assert same(res[0][:3], c["expected"]), (name, res[0])
+            rec["reference_cpu_ms"] = min(s["warm_ns"] for s in steps) * 1e-6
+            rec["reference_cpu_env"] = c["env"] or {}
+        if baseline.gpu_available() and not args.no_reference_gpu:
+            res = baseline.time_gpu([c["shape"]], [spec.adjacency], reps=1 if name == "G" else 3, env=c["env"])
+            assert same(res[0][:3], c["expected"]), (name, res[0])
+            rec["reference_cuda_ms"] = res[0][3] * 1e-6
+        out[name] = rec
+    return out
 
 
 def oracle_sample(specs, seconds):
-    """Oracle port on graphs taken in order until `seconds` of CPU work."""
+    """The oracle port on graphs taken in order until `seconds` of CPU work
+    (the CPU baseline where the reference library is not built)."""
     import oracle
     oracle.build()
     done, t0, results = 0, time.perf_counter(), []
@@ -199,113 +396,113 @@ def oracle_sample(specs, seconds):
     return done / dt, done, dt, results, oracle.threads()
 
 
-def run_reference(args):
-    rank, world, _ = dist_info()
-    if rank != 0:
-        return
-    shapes, specs = batch_workload(args.graphs)
-    # every step is a bounded sample of the batch (its first graphs, in order,
-    # for a fixed slice of CPU time), so the whole run stays near two minutes
-    per_step = min(2.0, 120.0 / max(1, args.steps + args.warmup))
-    for _ in range(args.warmup):
-        oracle_sample(specs, per_step)
-    total_done, total_s, cores = 0, 0.0, 1
-    for _ in range(args.steps):
-        _, done, dt, _, cores = oracle_sample(specs, per_step)
-        total_done += done
-        total_s += dt
-    v = total_done / total_s
-    line = {"metric": METRIC, "value": v, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * total_s / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "u64",
-            "data": "synthetic (reference generators, seeded)",
-            "impl": "reference", "config": {"workload": WORKLOAD, "graphs": len(specs)},
-            "cpu_baseline": {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
-                             "sample": "per step, the batch's first graphs for %.2f s of CPU time (%d graphs "
-                                       "over %d steps)" % (per_step, total_done, args.steps)},
-            "e2e": {"value": v, "unit": "evals/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line))
+def percentiles(v):
+    a = np.array(v) * 1e3
+    return {"p50": float(np.percentile(a, 50)), "p99": float(np.percentile(a, 99)), "mean": float(a.mean()),
+            "requests": len(v)}
 
 
-def serving(seconds, rate=20000.0):
+def serving(seconds, rate=20000.0, saturate_seconds=4.0):
     """The served annealing workload; returns the report dict."""
-    import threading
     import odp_gb300 as og
     from odp_gb300 import workloads
     shapes = workloads.chain_shapes(64)
     specs = workloads.build_graphs(shapes)
     srv = og.Server(lanes=4, max_batch=16, max_nodes=32768, memory_mb=4096)
     handles = [srv.register(og.GraphSpec(s.adjacency.copy(), nodes=s.nodes)) for s in specs]
-    think_mean = len(shapes) / rate
-    lat, done, lat_by_n = [], [0], {}
+    hosts = [s.adjacency.copy() for s in specs]
+    undos = [[] for _ in specs]
     lock = threading.Lock()
-    stop_at = [0.0]
-    checks = []
 
-    def chain(k):
-        sh, sp = shapes[k], specs[k]
-        n, d = sh["nodes"], sh["degree"]
-        host = sp.adjacency.copy()
-        rng = og.Rng(sh["proposal_seed"])
-        draw = np.random.default_rng(sh["proposal_seed"])
-        current = srv.wait(srv.submit(handles[k]))[2]
-        undo = []
-        local = []
-        while time.perf_counter() < stop_at[0]:
-            time.sleep(draw.exponential(think_mean))
-            r = rng.mutate_general(n, d, host)
-            res = srv.wait(srv.submit(handles[k], undo + og.two_opt_deltas(host, r, n)))
-            local.append(res[3])
-            delta = (res[2] - current) * n * (n - 1) / 2.0
-            if res[2] <= current or draw.random() < math.exp(-delta / 50.0):
-                current, undo = res[2], []
-            else:
-                og.Rng.restore_general(n, d, r, host)
-                undo = og.two_opt_deltas(host, r, n)
-        srv.wait(srv.submit(handles[k], undo))
-        with lock:
-            lat.extend(local)
-            lat_by_n.setdefault(n, []).extend(local)
-            done[0] += len(local)
-            if k < 4:
-                checks.append((k, host, res))
+    def run(chains, secs, think_mean):
+        lat, lat_by_n, stop_at = [], {}, time.perf_counter() + secs
 
-    threads = [threading.Thread(target=chain, args=(k,)) for k in range(len(shapes))]
-    t0 = time.perf_counter()
-    stop_at[0] = t0 + seconds
-    for t in threads:
-        t.start()
-    for t in threads:
-        t.join()
-    wall = time.perf_counter() - t0
+        def chain(k):
+            sh = shapes[k]
+            n, d = sh["nodes"], sh["degree"]
+            host = hosts[k]
+            rng = og.Rng(sh["proposal_seed"] + (7919 if think_mean == 0 else 0))
+            draw = np.random.default_rng(sh["proposal_seed"])
+            current = srv.wait(srv.submit(handles[k], undos[k]))[2]
+            undo, local = [], []
+            while time.perf_counter() < stop_at:
+                if think_mean > 0:
+                    time.sleep(draw.exponential(think_mean))
+                r = rng.mutate_general(n, d, host)
+                res = srv.wait(srv.submit(handles[k], undo + og.two_opt_deltas(host, r, n)))
+                local.append(res[3])
+                delta = (res[2] - current) * n * (n - 1) / 2.0
+                if res[2] <= current or draw.random() < math.exp(-delta / 50.0):
+                    current, undo = res[2], []
+                else:
+                    og.Rng.restore_general(n, d, r, host)
+                    undo = og.two_opt_deltas(host, r, n)
+            undos[k] = undo
+            with lock:
+                lat.extend(local)
+                lat_by_n.setdefault(n, []).extend(local)
+
+        threads = [threading.Thread(target=chain, args=(k,)) for k in chains]
+        t0 = time.perf_counter()
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        return time.perf_counter() - t0, lat, lat_by_n
+
+    wall, lat, lat_by_n = run(range(len(shapes)), seconds, len(shapes) / rate)
     st = srv.stats()
-    for k, host, res in checks:                      # the resident graphs followed the clients exactly
-        assert np.array_equal(srv.adjacency(handles[k]), host)
+    small = [k for k, s in enumerate(shapes) if s["nodes"] <= 8192]
+    sat_wall, sat_lat, sat_by_n = run(small, saturate_seconds, 0.0)
+    # every chain's resident graph followed its client, and its served result
+    # equals the same graph evaluated alone, bit for bit
+    finals = [srv.wait(srv.submit(handles[k], undos[k])) for k in range(len(shapes))]
+    for k in range(len(shapes)):
+        assert np.array_equal(srv.adjacency(handles[k]), hosts[k])
     srv.close()
-    lat_ms = np.array(lat) * 1e3
-    # the same proposals one call at a time: ODP_Set_aspl per proposal, as the reference's annealing samples do
-    pc = []
-    for sh, sp in zip(shapes[:12], specs[:12]):
-        og.init_aspl_general(sh["nodes"], sh["degree"])
-        og.set_aspl(sp.adjacency)
-        t1 = time.perf_counter()
-        for _ in range(3):
-            og.set_aspl(sp.adjacency)
-        pc.append((time.perf_counter() - t1) / 3)
-        og.finalize_aspl()
+    alone = og.Batch([og.GraphSpec(hosts[k], nodes=shapes[k]["nodes"]) for k in range(len(shapes))])
+    ares = alone.run()
+    alone.close()
+    checked = {}
+    for k, (f, a) in enumerate(zip(finals, ares)):
+        assert same(f[:3], a), ("served and alone differ", k, f, a)
+        checked[str(shapes[k]["nodes"])] = checked.get(str(shapes[k]["nodes"]), 0) + 1
+    # one call at a time: ODP_Set_aspl per proposal, as the reference's annealing samples do
+    per_call_ms = {}
+    for n in sorted({s["nodes"] for s in shapes}):
+        ts = []
+        for k in [i for i, s in enumerate(shapes) if s["nodes"] == n][:3]:
+            og.init_aspl_general(n, shapes[k]["degree"])
+            og.set_aspl(hosts[k])
+            t1 = time.perf_counter()
+            for _ in range(5):
+                og.set_aspl(hosts[k])
+            ts.append((time.perf_counter() - t1) / 5)
+            og.finalize_aspl()
+        per_call_ms[n] = float(np.mean(ts)) * 1e3
+
+    def same_mix(by_n):
+        cnt = sum(len(v) for v in by_n.values())
+        return cnt / sum(len(v) * per_call_ms[n] * 1e-3 for n, v in by_n.items())
+
+    done, sat_done = len(lat), len(sat_lat)
     return {"workload": "64 annealing chains, n in {1024,4096,16384,32768}, d in {8,16,24}, 2-opt proposals, "
                         "closed loop (1 outstanding per chain), exponential think time for a %d req/s offered cap"
                         % int(rate),
-            "seconds": wall, "completed": done[0], "evals_per_s": done[0] / wall,
-            "offered_cap_req_per_s": rate,
-            "latency_ms": {"p50": float(np.percentile(lat_ms, 50)), "p99": float(np.percentile(lat_ms, 99)),
-                           "mean": float(lat_ms.mean())},
-            "latency_ms_by_n": {str(k): {"p50": float(np.percentile(np.array(v) * 1e3, 50)),
-                                         "p99": float(np.percentile(np.array(v) * 1e3, 99)), "requests": len(v)}
-                                for k, v in sorted(lat_by_n.items())},
+            "seconds": wall, "completed": done, "evals_per_s": done / wall, "offered_cap_req_per_s": rate,
+            "latency_ms": percentiles(lat),
+            "latency_ms_by_n": {str(k): percentiles(v) for k, v in sorted(lat_by_n.items())},
+            "evals_per_s_by_n": {str(k): len(v) / wall for k, v in sorted(lat_by_n.items())},
+            "per_call_ms_by_n": {str(k): v for k, v in per_call_ms.items()},
+            "per_call_evals_per_s_same_mix": same_mix(lat_by_n),
             "batches": st["batches"], "mean_batch": st["batched_requests"] / max(1, st["batches"]),
             "max_batch": st["max_batch"], "max_concurrent_lanes": st["max_inflight_lanes"],
-            "per_call_evals_per_s_same_mix": 1.0 / float(np.mean(pc)),
+            "saturating_small": {"workload": "the %d chains with n <= 8192, no think time" % len(small),
+                                 "seconds": sat_wall, "completed": sat_done, "evals_per_s": sat_done / sat_wall,
+                                 "latency_ms": percentiles(sat_lat),
+                                 "per_call_evals_per_s_same_mix": same_mix(sat_by_n),
+                                 "served_over_per_call": (sat_done / sat_wall) / same_mix(sat_by_n)},
+            "results_checked_alone_by_n": checked,
             "note": "the offered cap exceeds what any GPU can serve for n=32768 chains; chains are closed loop"}
 
 
@@ -365,18 +562,20 @@ def anneal(seconds, temperature=50.0):
             "accepted": accepted}
 
 
-def same(a, b):
-    return a[0] == b[0] and a[1] == b[1] and float(a[2]).hex() == float(b[2]).hex()
-
-
 def run_own(args):
     rank, world, local = dist_info()
     dist = Dist(world)
     import odp_gb300 as og
+    import baseline
     og.load()
     shapes, specs = batch_workload(args.graphs)
     count = len(specs)
+    if count == 512 and adjacency_sha([s.adjacency for s in specs]) != BATCH_SHA256:
+        raise RuntimeError("the batch's graphs differ from the reference generators'")
     adj_bytes = int(sum(s.adjacency.nbytes for s in specs))
+    peaks, peak_src = measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    l2_gbs = og.measure_l2_read_gbs(48, 40)
 
     # ---- autotune the schedule for this batch (outside every timed region) ----
     from odp_gb300 import autotune
@@ -411,15 +610,14 @@ def run_own(args):
     line = {"metric": METRIC, "value": value, "unit": "evals/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u64", "data": "synthetic (reference generators, seeded)",
-            "config": {"workload": WORKLOAD, "graphs": count, "jobs": info["njobs"], "slots": info["nslots"],
-                       "l2": "flushed (%d MB write) before every timed run" % args.flush_mb,
-                       "parallelism": "replicas" if world > 1 else "single"},
+            "config": common_config(count),
+            "schedule": {"jobs": info["njobs"], "slots": info["nslots"],
+                         "parallelism": "replicas" if world > 1 else "single"},
             "e2e": {"value": world * count / e2e_s, "unit": "evals/s", "h2d_bytes_per_step": adj_bytes,
                     "d2h_bytes_per_step": 16 * count + 128},
             "gpu_launches": args.steps,
             "batch_device_ms_with_transfers": ms_full,
             "autotune": tune_report}
-
     autotune.clear()
 
     # ---- one graph per call on the same GPU ----
@@ -448,36 +646,47 @@ def run_own(args):
             og.set_aspl(s.adjacency)
             og.finalize_aspl()
         dropin_s = (time.perf_counter() - t0) / k
-        line["per_call"] = {"evals_per_s": count / pc_s, "form": "one plan per graph, ODPX_Batch_run each",
-                            "drop_in_init_set_finalize_evals_per_s": 1.0 / dropin_s,
-                            "batched_e2e_over_per_call": (count / e2e_s) / (count / pc_s),
-                            "batched_device_over_per_call": (count * 1000.0 / ms) / (count / pc_s),
-                            "reference_cuda_per_call": "unavailable: the reference CUDA library cannot be "
-                                                       "built on the GPU host (its sources are not there)"}
+        e2e_v = count / e2e_s
+        pcd = {"evals_per_s": count / pc_s, "form": "one plan per graph, ODPX_Batch_run each",
+               "drop_in_init_set_finalize_evals_per_s": 1.0 / dropin_s,
+               "batched_e2e_over_per_call": e2e_v / (count / pc_s),
+               "batched_device_over_per_call": (count * 1000.0 / ms) / (count / pc_s)}
+        if baseline.gpu_available() and not args.no_reference_gpu:
+            rg = baseline.time_gpu(shapes, [s.adjacency for s in specs], reps=2)
+            assert all(same(a, b[:3]) for a, b in zip(res, rg)), "reference CUDA library and batch differ"
+            ref_s = sum(r[3] for r in rg) * 1e-9
+            pcd["reference_cuda_per_call"] = {
+                "evals_per_s": count / ref_s,
+                "form": "the reference's libodp_cuda.a built from its sources for sm_103a, in its own process: "
+                        "per graph Init, an untimed and 2 timed ODP_Set_aspl (mean), Finalize",
+                "results_equal_batch": True}
+            pcd["batched_e2e_over_faster_per_call"] = e2e_v / max(count / pc_s, count / ref_s)
+        else:
+            pcd["reference_cuda_per_call"] = "unavailable: the reference CUDA library was not built here"
+        line["per_call"] = pcd
 
-    # ---- the single large graph (MATRIX_SAVING configuration) ----
+    # ---- the reference's configurations, one graph each ----
+    l2_bytes = 126.5e6
+    if not args.no_configs:
+        line["configs"] = time_configs(args, l2_gbs, hbm, l2_bytes)
+
+    # ---- the single large graph (MATRIX_SAVING configuration), autotuned ----
     if not args.no_single:
-        adj = single_graph()
-        single_tune = autotune.tune_single(og.GraphSpec(adj, nodes=C2["nodes"])) if not args.no_tune else None
-        sb = og.Batch([og.GraphSpec(adj, nodes=C2["nodes"])])
+        c2 = [c for c in config_graphs() if c["name"] == "C2"][0]
+        spec = c2["spec"]
+        single_tune = autotune.tune_single(spec) if not args.no_tune else None
+        sb = og.Batch([spec])
         r = sb.run()[0]
-        assert r[:2] == C2["result"], r
+        assert same(r, c2["expected"]), r
         sb.time(2, mode=1, flush_mb=args.flush_mb)
         sms = sb.time(max(3, args.steps // 2), mode=1, flush_mb=args.flush_mb)
         sbytes = sb.bytes_alg()
         sinfo = sb.info(0)
         sb.close()
-        og.init_aspl_general(C2["nodes"], C2["degree"])
-        og.set_aspl(adj)
-        t0 = time.perf_counter()
-        for _ in range(max(3, args.steps // 2)):
-            og.set_aspl(adj)
-        s_e2e = (time.perf_counter() - t0) / max(3, args.steps // 2)
-        og.finalize_aspl()
-        line["single_graph"] = {"workload": "n=65536 d=16 seed=2 (MATRIX_SAVING config)", "evals_per_s": 1000.0 / sms,
-                                "ms": sms, "e2e_evals_per_s": 1.0 / s_e2e, "bytes_alg": sbytes,
-                                "achieved_gbs": sbytes / (sms * 1e-3) / 1e9, "chunk_words": 1 << sinfo["wc_log2"],
-                                "slots": sinfo["nslots"], "tile_rows": sinfo["tile_rows"], "autotune": single_tune,
+        line["single_graph"] = {"workload": c2["workload"] + " (autotuned)", "evals_per_s": 1000.0 / sms,
+                                "ms": sms, "bytes_alg": sbytes, "achieved_alg_gbs": sbytes / (sms * 1e-3) / 1e9,
+                                "chunk_words": 1 << sinfo["wc_log2"], "slots": sinfo["nslots"],
+                                "tile_rows": sinfo["tile_rows"], "autotune": single_tune,
                                 "result": {"diameter": r[0], "sum": r[1], "ASPL": r[2]}}
         autotune.clear()
 
@@ -486,28 +695,46 @@ def run_own(args):
     if not args.no_anneal and world == 1:
         line["anneal"] = anneal(args.serve_seconds)
 
-    peaks, src = measured_peaks()
-    hbm = float(peaks.get("hbm_gbs", 6800.0))
-    l2 = og.measure_l2_read_gbs(48, 40)
-    achieved = balg / (ms * 1e-3) / 1e9
-    traffic = NCU_DRAM["bytes"] * balg / NCU_DRAM["bytes_alg"]
-    line["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                        "traffic": traffic, "peak_source": src + " (MEASURED_PEAKS.json hbm_gbs)",
-                        "traffic_source": "ncu DRAM bytes of one launch on the first %d graphs, scaled by algorithmic "
-                                          "bytes" % NCU_DRAM["graphs"],
-                        "bytes_alg_per_launch": balg, "l2_read_peak_measured": l2,
-                        "frac_of_l2_read_peak": achieved / l2 if l2 > 0 else None}
-    moved = NCU_DRAM["l2_read_bytes"] * balg / NCU_DRAM["bytes_alg"]
-    line["roofline"].update({"l2_read_bytes_per_launch": moved, "l2_read_gbs": moved / (ms * 1e-3) / 1e9,
-                             "l2_read_frac_of_l2_read_peak": moved / (ms * 1e-3) / 1e9 / l2 if l2 > 0 else None,
-                             "l2_read_source": "ncu L2-to-SM read bytes of one launch on the first %d graphs, scaled "
-                                               "by algorithmic bytes" % NCU_DRAM["graphs"]})
+    # ---- roofline of the headline kernel: the batched engine against L2 ----
+    rat = NCU_RATIOS["batch"]
+    moved = balg * rat["l2_read"]
+    achieved = moved / (ms * 1e-3) / 1e9
+    line["roofline"] = {"bound": "l2", "achieved": achieved, "peak": l2_gbs, "unit": "GB/s",
+                        "frac": achieved / l2_gbs, "traffic": balg * rat["dram"],
+                        "kernel": "engine_kernel",
+                        "achieved_source": "bytes read from L2 by the SMs per launch (ncu "
+                                           "l1tex__m_xbar2l1tex_read_bytes.sum per algorithmic byte, one launch on "
+                                           "the first 128 graphs, times this launch's algorithmic bytes) / the "
+                                           "launch's CUDA-event time",
+                        "peak_source": "L2 read ceiling measured live in this run by a streaming probe of 16-byte "
+                                       "L2-only loads over a 48 MB L2-resident buffer (MEASURED_PEAKS.json has no "
+                                       "L2 figure)",
+                        "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum per algorithmic byte, "
+                                          "same capture, times this launch's algorithmic bytes",
+                        "bytes_alg_per_launch": balg, "alg_gbs": balg / (ms * 1e-3) / 1e9,
+                        "alg_frac_of_l2_peak": balg / (ms * 1e-3) / 1e9 / l2_gbs,
+                        "dram_gbs": balg * rat["dram"] / (ms * 1e-3) / 1e9,
+                        "dram_frac_of_hbm": balg * rat["dram"] / (ms * 1e-3) / 1e9 / hbm,
+                        "hbm_peak": hbm, "hbm_peak_source": peak_src + " (MEASURED_PEAKS.json hbm_gbs)"}
     line["clocks"] = clk.summary()
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        v, done, dt, cres, cores = oracle_sample(specs, args.cpu_seconds)
-        assert all(same(a, b) for a, b in zip(res[:done], cres)), "GPU and oracle differ"
-        line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
-                                "sample": "first %d graphs of the batch, %.1f s" % (done, dt)}
+        host = baseline.host_description()
+        if baseline.cpu_available():
+            steps, cres = baseline.time_cpu(shapes, [s.adjacency for s in specs], steps=1, warmup=0, sets=2)
+            assert all(same(a, b[:3]) for a, b in zip(res, cres)), "GPU and reference CPU library differ"
+            v = count / (steps[0]["warm_ns"] * 1e-9)
+            line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": host["nproc"], "kind": "reference",
+                                    "cpu_model": host["cpu_model"], "nproc": host["nproc"],
+                                    "sample": "the whole batch once: per graph a forked child of libodp_threads.a "
+                                              "(Init, an untimed and a timed ODP_Set_aspl, Finalize), "
+                                              "OMP_NUM_THREADS=%d; %.2f s of timed Set calls"
+                                              % (host["nproc"], steps[0]["warm_ns"] * 1e-9)}
+        else:
+            v, done, dt, cres, cores = oracle_sample(specs, 10.0)
+            assert all(same(a, b) for a, b in zip(res[:done], cres)), "GPU and oracle differ"
+            line["cpu_baseline"] = {"value": v, "unit": "evals/s", "cores": cores, "kind": "port",
+                                    "cpu_model": host["cpu_model"], "nproc": host["nproc"],
+                                    "sample": "first %d graphs of the batch, %.1f s" % (done, dt)}
     if rank == 0:
         print(json.dumps(line))
 

@@ -7,9 +7,11 @@ Two checkers live here; the product (odp_gb300) never imports this package.
   ``oracle/_build/liboracle.so`` and called through :func:`aspl`.  It runs
   anywhere gcc does, including the GPU host.
 * ``oracle/_ref/``: the reference CPU library itself (libodp.a /
-  libodp_threads.a) compiled from the reference sources by ``oracle/Makefile``
-  where that tree is present, driven through ``ref_driver``.  Used to pin the
-  restatement and to generate the committed golden fixtures.
+  libodp_threads.a) compiled by ``oracle/Makefile`` from the reference's own
+  sources, as ``baseline/install_ref.sh`` installs them into
+  ``baseline/_ref/src`` (git-ignored, so they travel with the working tree),
+  driven through ``ref_driver``.  Used to pin the restatement and to generate
+  the committed golden fixtures.
 """
 import ctypes
 import os
@@ -21,7 +23,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REF_SOURCE = os.environ.get("ODP_REFERENCE_DIR", "/root/reference")
+ROOT = os.path.dirname(HERE)
+REF_SOURCE = os.path.join(ROOT, "baseline", "_ref", "src")
 
 KIND_DEFAULT, KIND_MATRIX, KIND_SAVING = 0, 1, 2
 
@@ -35,7 +38,12 @@ def build(force=False):
         subprocess.run(["gcc", "-O3", "-std=gnu11", "-fopenmp", "-fPIC", "-shared", "-o", tmp, src],
                        check=True)
         os.replace(tmp, LIB)
-    if os.path.isdir(REF_SOURCE):
+    import sys
+    if ROOT not in sys.path:
+        sys.path.insert(0, ROOT)
+    import baseline
+    baseline.install()
+    if baseline.sources_present():
         subprocess.run(["make", "-s", "-C", HERE, "ref", "REF=" + REF_SOURCE], check=True,
                        stdout=subprocess.DEVNULL)
     return LIB

@@ -24,8 +24,7 @@ def test_reference_arm_under_torchrun_prints_once():
     pytest.importorskip("torch")
     cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
            "--master-addr", "127.0.0.1", "--master-port", str(free_port()), os.path.join(ROOT, "bench.py"),
-           "--impl", "reference", "--gpus", "2", "--graphs", "12", "--steps", "1", "--warmup", "1",
-           "--cpu-seconds", "0.5"]
+           "--impl", "reference", "--gpus", "2", "--graphs", "12", "--steps", "1", "--warmup", "1"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=280, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -67,7 +66,7 @@ def test_reference_arm_json_line_carries_the_contract_keys():
     contract, its cpu_baseline describes this run, and its e2e moves no
     bytes (the work runs on the host)."""
     cmd = [sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--graphs", "12", "--steps", "2",
-           "--warmup", "3", "--cpu-seconds", "0.5"]
+           "--warmup", "3"]
     r = subprocess.run(cmd, capture_output=True, text=True, timeout=280, cwd=ROOT)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
@@ -78,7 +77,9 @@ def test_reference_arm_json_line_carries_the_contract_keys():
         assert k in rec, k
     assert rec["impl"] == "reference" and rec["steps"] == 2 and rec["warmup"] == 3 and rec["n_gpus"] == 1
     assert rec["higher_is_better"] is True and rec["value"] > 0 and rec["ms_per_step"] > 0
-    assert "workload" in rec["config"]
+    import bench
+    assert rec["config"] == bench.common_config(12)          # the same config as the GPU arm's line
+    assert rec["reference"]["odp_gb300_mapped"] is False
     cb = rec["cpu_baseline"]
     assert cb["value"] == rec["value"] and cb["unit"] == rec["unit"] and cb["cores"] >= 1
     assert cb["kind"] in ("reference", "port") and cb["sample"]
