@@ -1234,7 +1234,9 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   /* The array keeps whatever the previous call left in it: the engine state
    * is rewritten here in full; the neighbour table and the bitset buffers
    * are overwritten by the kernels before they are read. */
-  unsigned char state[sizeof(gbx_slot) * 2 + sizeof(gbx_ctrl) + 64 + 64 + sizeof(gbx_job_out) * NOALLOC_MAX_JOBS];
+  /* aligned for the gbx_slot / gbx_ctrl / gbx_job_out views taken of it */
+  alignas(64) unsigned char state[sizeof(gbx_slot) * 2 + sizeof(gbx_ctrl) + 64 + 64 +
+                                  sizeof(gbx_job_out) * NOALLOC_MAX_JOBS];
   memset(state, 0, sizeof(state));
   gbx_slot *sl = (gbx_slot *)state;
   unsigned long long *bufs = (unsigned long long *)(base + off_buf);
@@ -1266,7 +1268,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
       (gbx_ctrl *)(base + off_state + out_off), (gbx_graph_acc *)(base + off_state + acc_off),
       (gbx_job_out *)(base + off_state + levels_off), 60ull * 1000000000ull);
   if(cudaGetLastError() != cudaSuccess) return ODPX_ERR_CUDA;
-  unsigned char out[sizeof(gbx_ctrl) + 64 + 64];
+  alignas(64) unsigned char out[sizeof(gbx_ctrl) + 64 + 64];
   if(cudaMemcpyAsync(out, base + off_state + out_off, sizeof(out), cudaMemcpyDeviceToHost, st) ||
      cudaStreamSynchronize(st))
     return ODPX_ERR_CUDA;

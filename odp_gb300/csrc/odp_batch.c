@@ -257,7 +257,14 @@ int ODPX_Batch_job_profile(const ODPX_Batch *batch, int *graph, double *loaded_u
 
 void ODPX_Batch_set_wait_limit(ODPX_Batch *batch, unsigned long long ns)
 {
-  if(batch) batch->spin_limit_ns = ns;
+  if(!batch || batch->spin_limit_ns == ns) return;
+  batch->spin_limit_ns = ns;
+  /* the limit is an argument of the captured engine launch: capture anew */
+  if(batch->graph_exec){
+    gbx_stream_sync(batch->stream);
+    gbx_graph_destroy(batch->graph_exec);
+    batch->graph_exec = NULL;
+  }
 }
 
 double ODPX_Batch_bytes_alg(const ODPX_Batch *batch) { return batch ? odp_plan_bytes_alg(batch) : 0.0; }

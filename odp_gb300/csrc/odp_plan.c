@@ -320,7 +320,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
    * plan with few jobs more of them (the n = 1024, d = 8 graph: 2 jobs of 8
    * words, or 8 of 2 words, each gathering a quarter of the bytes), until the
    * jobs cover the SMs. */
-  const int sms = gbx_engine_blocks(0) / 4 > 0 ? gbx_engine_blocks(0) / 4 : 1;
+  const int sms = g_sm_count > 0 ? g_sm_count : 1;
   if(small && small_jobs > sms) small = 0;
   if(small){
     while(small_jobs < sms){
@@ -330,7 +330,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       if(k < 0) break;
       const int n = shapes[k].grid ? shapes[k].width * shapes[k].height : shapes[k].nodes;
       const int W = (n / shapes[k].symmetries + 63) / 64;
-      small_jobs += ((W + (1 << (small_wl[k] - 1)) - 1) >> (small_wl[k] - 1)) - ((W + (1 << small_wl[k]) - 1) >> small_wl[k]);
+      const long long more = ((W + (1 << (small_wl[k] - 1)) - 1) >> (small_wl[k] - 1)) -
+                             ((W + (1 << small_wl[k]) - 1) >> small_wl[k]);
+      if(small_jobs + more > sms) break;       /* halving this graph's chunks would pass one job per SM */
+      small_jobs += more;
       small_wl[k]--;
     }
   }

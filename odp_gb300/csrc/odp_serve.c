@@ -383,6 +383,9 @@ int ODPX_Serve_create(const ODPX_Serve_config *cfg, ODPX_Server **out)
   int slots_total = (int)((double)c.memory_mb * 1024.0 * 1024.0 / per_slot);
   int per_lane = slots_total / c.lanes;
   if(per_lane < 1){
+    pthread_mutex_destroy(&s->mu);
+    pthread_cond_destroy(&s->cv_work);
+    pthread_cond_destroy(&s->cv_done);
     free(s);
     return ODPX_ERR_MEMORY;
   }
@@ -404,10 +407,19 @@ int ODPX_Serve_create(const ODPX_Serve_config *cfg, ODPX_Server **out)
       return e;
     }
   }
-  if(gbx_stream_create(&s->ctl_stream)) return ODPX_ERR_CUDA;
+  /* from here on a failure releases everything through ODPX_Serve_destroy,
+   * which handles a server whose scheduler thread never started */
+  if(gbx_stream_create(&s->ctl_stream)){
+    s->ctl_stream = NULL;
+    ODPX_Serve_destroy(s);
+    return ODPX_ERR_CUDA;
+  }
   s->stats.slots_per_lane = per_lane;
   s->stats.blocks_per_lane = blocks;
-  if(pthread_create(&s->thread, NULL, scheduler, s) != 0) return ODPX_ERR_STATE;
+  if(pthread_create(&s->thread, NULL, scheduler, s) != 0){
+    ODPX_Serve_destroy(s);
+    return ODPX_ERR_STATE;
+  }
   s->started = 1;
   *out = s;
   return 0;

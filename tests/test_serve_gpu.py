@@ -136,3 +136,47 @@ def test_delta_past_a_rows_degree_is_refused():
         b.close()
     assert same(got, oracle.aspl(host, nodes=n, num_degrees=deg))
     srv.close()
+
+
+def test_served_results_at_the_served_sizes():
+    """The served workload's large chains (n = 16384 and 32768, d = 24) share
+    lanes, slots and L2 with small ones: every result must still equal the
+    same graph evaluated alone, and the oracle at two of the steps."""
+    sizes = [(16384, 24), (32768, 24), (1024, 8), (4096, 16), (2048, 8), (32768, 8)]
+    chains = []
+    for i, (n, d) in enumerate(sizes):
+        chains.append((n, d, og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=1000 + i), d)))
+    srv = og.Server(lanes=4, max_batch=16, max_nodes=32768, memory_mb=4096)
+    handles = [srv.register(og.GraphSpec(adj.copy(), nodes=n)) for n, d, adj in chains]
+    steps = 8
+    results, errors = {}, []
+
+    def run_chain(k):
+        try:
+            n, d, adj = chains[k]
+            host = adj.copy()
+            rng = og.Rng(2000 + k)
+            for step in range(steps):
+                r = rng.mutate_general(n, d, host)
+                got = srv.wait(srv.submit(handles[k], og.two_opt_deltas(host, r, n)))
+                results[(k, step)] = (got[:3], host.copy())
+        except Exception as e:       # surfaced below
+            errors.append(e)
+
+    threads = [threading.Thread(target=run_chain, args=(k,)) for k in range(len(chains))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors
+    st = srv.stats()
+    srv.close()
+    assert st["requests_done"] == len(chains) * steps
+    for k, (n, d, adj) in enumerate(chains):
+        b = og.Batch([og.GraphSpec(adj, nodes=n)])
+        for step in range(steps):
+            got, host = results[(k, step)]
+            assert same(got, b.run([host])[0]), (n, d, step)
+            if n >= 16384 and step in (3, steps - 1):
+                assert same(got, oracle.aspl(host, nodes=n)), (n, d, step)
+        b.close()
