@@ -12,6 +12,7 @@ driver, runs it, and parses what it prints.  It never loads libodp_gb300.
 import os
 import shutil
 import subprocess
+import sys
 import tempfile
 import threading
 
@@ -59,11 +60,11 @@ def build(cpu=True, gpu=True):
     targets = (["cpu"] if cpu else []) + (["gpu"] if gpu else [])
     ok = {}
     for t in targets:
-        r = subprocess.run(["make", "-s", "-C", HERE, t], stdout=subprocess.DEVNULL, stderr=subprocess.PIPE,
+        r = subprocess.run(["make", "-s", "-C", HERE, t], stdout=subprocess.PIPE, stderr=subprocess.STDOUT,
                            text=True)
         ok[t] = r.returncode == 0
         if r.returncode != 0:
-            ok[t + "_error"] = r.stderr[-2000:]
+            sys.stderr.write("baseline: make %s failed:\n%s\n" % (t, r.stdout[-3000:]))
     return ok.get("cpu", False), ok.get("gpu", False)
 
 

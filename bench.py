@@ -64,14 +64,18 @@ L2_NOTE = "GPU arm: L2 flushed (512 MB write) before every timed device run"
 # same for the reference generators (baseline/ref_bench.c gen) and the
 # library's own; both arms check it, so they evaluate identical graphs.
 BATCH_SHA256 = "cb594241cefc45d1"
-# ncu counters of one engine_kernel launch at this build and schedule, per
-# algorithmic byte of the same launch (ncu --metrics dram__bytes_read.sum,
-# dram__bytes_write.sum, l1tex__m_xbar2l1tex_read_bytes.sum; bytes_alg from
-# ODPX_Batch_bytes_alg): "batch" on the first 128 graphs of the batch, "C2"..
-# on the configuration graphs.  A launch's L2 read bytes and DRAM traffic are
-# taken as its algorithmic bytes times these ratios.
+# ncu counters of one engine_kernel launch per leg, per algorithmic byte of the
+# same launch (ncu --metrics dram__bytes_read.sum, dram__bytes_write.sum,
+# l1tex__m_xbar2l1tex_read_bytes.sum, one launch per leg selected by its NVTX
+# range, bytes_alg from ODPX_Batch_bytes_alg; profiles/engine_kernel_ratios.md):
+# "batch" is the 512-graph batch with the saved autotuned schedule, C2, C3 and
+# G the configuration graphs with the default schedule.  A launch's L2 read
+# bytes and DRAM traffic are taken as its algorithmic bytes times these ratios.
 NCU_RATIOS = {
-    "batch": {"l2_read": 14874844864.0 / 24803482864.0, "dram": (936275200.0 + 815841024.0) / 24803482864.0},
+    "batch": {"l2_read": 0.572758, "dram": 0.108146},
+    "C2": {"l2_read": 0.654676, "dram": 0.108437},
+    "C3": {"l2_read": 0.784851, "dram": 0.205265},
+    "G": {"l2_read": 0.194935, "dram": 0.047269},
 }
 
 
@@ -92,7 +96,32 @@ def parse():
     p.add_argument("--no-anneal", action="store_true")
     p.add_argument("--no-tune", action="store_true")
     p.add_argument("--serve-seconds", type=float, default=8.0)
+    p.add_argument("--configs", default="C1,C2,C3,G", help="configurations to time (comma list)")
+    p.add_argument("--save-tuning", default=None, help="write the batch autotuner's result to this file")
+    p.add_argument("--tuning-file", default=None, help="install this saved batch tuning instead of tuning")
+    p.add_argument("--nvtx", action="store_true",
+                   help="after each leg, one more launch inside an NVTX range named after the leg (batch, C1, C2, "
+                        "C3, G, single), for profilers")
     return p.parse_args()
+
+
+class NvtxLeg:
+    """An NVTX push/pop range around one profiling launch (no-op unless enabled)."""
+
+    def __init__(self, enabled):
+        self.nvtx = None
+        if enabled:
+            import torch
+            self.nvtx = torch.cuda.nvtx
+
+    def run(self, name, fn):
+        if self.nvtx is None:
+            return
+        self.nvtx.range_push(name)
+        try:
+            fn()
+        finally:
+            self.nvtx.range_pop()
 
 
 def dist_info():
@@ -321,13 +350,16 @@ def live_bytes(spec, info):
     return 2.0 * info["nslots"] * n * 8.0 * (1 << info["wc_log2"])
 
 
-def time_configs(args, l2_gbs, hbm_gbs, l2_bytes):
+def time_configs(args, l2_gbs, hbm_gbs, l2_bytes, nvtx):
     import odp_gb300 as og
     import baseline
     out = {}
     reps = {"C1": 200, "C2": 10, "C3": 20, "G": 4}
+    wanted = set(args.configs.split(","))
     for c in config_graphs():
         spec, name = c["spec"], c["name"]
+        if name not in wanted:
+            continue
         b = og.Batch([spec])
         r = b.run()[0]
         assert same(r, c["expected"]), (name, r, c["expected"])
@@ -336,6 +368,7 @@ def time_configs(args, l2_gbs, hbm_gbs, l2_bytes):
         balg = b.bytes_alg()
         info = b.info(0)
         kernel = b.kernel()
+        nvtx.run(name, lambda: b.time(1, mode=1, flush_mb=args.flush_mb))
         b.close()
         # ODP_Set_aspl end to end: host adjacency, copies and decode included
         nd = None
@@ -356,15 +389,20 @@ def time_configs(args, l2_gbs, hbm_gbs, l2_bytes):
         live = live_bytes(spec, info)
         rec = {"workload": c["workload"], "kernel": kernel, "device_ms": ms, "set_aspl_e2e_ms": e2e_ms,
                "bytes_alg": balg, "alg_gbs": balg / (ms * 1e-3) / 1e9, "live_bitset_bytes": live,
-               "bound": "l2" if live <= l2_bytes else "hbm",
+               "schedule": {"chunk_words": 1 << info["wc_log2"], "jobs": info["njobs"], "slots": info["nslots"],
+                            "tile_rows": info["tile_rows"]},
                "result": {"diameter": r[0], "sum": r[1], "ASPL": r[2]}}
         ratio = NCU_RATIOS.get(name)
         if ratio:
-            moved = balg * ratio["l2_read"]
-            rec.update({"l2_read_bytes": moved, "l2_read_gbs": moved / (ms * 1e-3) / 1e9,
-                        "l2_read_frac": moved / (ms * 1e-3) / 1e9 / l2_gbs,
-                        "dram_bytes": balg * ratio["dram"],
-                        "dram_frac_of_hbm": balg * ratio["dram"] / (ms * 1e-3) / 1e9 / hbm_gbs})
+            # the bound is whichever of L2 reads and DRAM traffic is nearer its ceiling
+            moved, dram = balg * ratio["l2_read"], balg * ratio["dram"]
+            l2f = moved / (ms * 1e-3) / 1e9 / l2_gbs
+            dramf = dram / (ms * 1e-3) / 1e9 / hbm_gbs
+            rec.update({"l2_read_bytes": moved, "l2_read_gbs": moved / (ms * 1e-3) / 1e9, "l2_read_frac": l2f,
+                        "dram_bytes": dram, "dram_gbs": dram / (ms * 1e-3) / 1e9, "dram_frac_of_hbm": dramf,
+                        "bound": "l2" if l2f >= dramf else "hbm", "frac": max(l2f, dramf)})
+        else:
+            rec["bound"] = "l2" if live <= l2_bytes else "hbm"
         if baseline.cpu_available() and not args.no_cpu_baseline:
             sets = 1 if name == "G" else 2
             steps, res = baseline.time_cpu([c["shape"]], [spec.adjacency], steps=1 if name in ("G", "C2", "C3")
@@ -579,7 +617,17 @@ def run_own(args):
 
     # ---- autotune the schedule for this batch (outside every timed region) ----
     from odp_gb300 import autotune
-    tune_report = autotune.tune_batch(specs) if not args.no_tune else None
+    nvtx = NvtxLeg(args.nvtx)
+    if args.tuning_file:
+        with open(args.tuning_file) as f:
+            tune_report = json.load(f)
+        autotune.apply(tune_report)
+        tune_report = dict(tune_report, loaded_from=args.tuning_file)
+    else:
+        tune_report = autotune.tune_batch(specs) if not args.no_tune else None
+    if args.save_tuning and tune_report is not None:
+        with open(args.save_tuning, "w") as f:
+            json.dump(tune_report, f)
 
     # ---- batched engine on resident inputs (headline) ----
     batch = og.Batch(specs)
@@ -594,6 +642,7 @@ def run_own(args):
     value = world * count * 1000.0 / ms
     balg = batch.bytes_alg()
     info = batch.info(0)
+    nvtx.run("batch", lambda: batch.time(1, mode=1, flush_mb=args.flush_mb))
     ms_full = batch.time(max(3, args.steps // 4), mode=0, flush_mb=args.flush_mb)
 
     # ---- end to end through ODP_Set_aspl_batch (host adjacency) ----
@@ -668,7 +717,7 @@ def run_own(args):
     # ---- the reference's configurations, one graph each ----
     l2_bytes = 126.5e6
     if not args.no_configs:
-        line["configs"] = time_configs(args, l2_gbs, hbm, l2_bytes)
+        line["configs"] = time_configs(args, l2_gbs, hbm, l2_bytes, nvtx)
 
     # ---- the single large graph (MATRIX_SAVING configuration), autotuned ----
     if not args.no_single:
@@ -682,6 +731,7 @@ def run_own(args):
         sms = sb.time(max(3, args.steps // 2), mode=1, flush_mb=args.flush_mb)
         sbytes = sb.bytes_alg()
         sinfo = sb.info(0)
+        nvtx.run("single", lambda: sb.time(1, mode=1, flush_mb=args.flush_mb))
         sb.close()
         line["single_graph"] = {"workload": c2["workload"] + " (autotuned)", "evals_per_s": 1000.0 / sms,
                                 "ms": sms, "bytes_alg": sbytes, "achieved_alg_gbs": sbytes / (sms * 1e-3) / 1e9,
@@ -703,8 +753,8 @@ def run_own(args):
                         "frac": achieved / l2_gbs, "traffic": balg * rat["dram"],
                         "kernel": "engine_kernel",
                         "achieved_source": "bytes read from L2 by the SMs per launch (ncu "
-                                           "l1tex__m_xbar2l1tex_read_bytes.sum per algorithmic byte, one launch on "
-                                           "the first 128 graphs, times this launch's algorithmic bytes) / the "
+                                           "l1tex__m_xbar2l1tex_read_bytes.sum per algorithmic byte, one launch of "
+                                           "the tuned 512-graph batch, times this launch's algorithmic bytes) / the "
                                            "launch's CUDA-event time",
                         "peak_source": "L2 read ceiling measured live in this run by a streaming probe of 16-byte "
                                        "L2-only loads over a 48 MB L2-resident buffer (MEASURED_PEAKS.json has no "

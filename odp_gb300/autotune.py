@@ -145,3 +145,12 @@ def tune_single(spec, widths=(3, 4, 5, 6), slots=(2, 4, 8, 16, 32), tile_kb=(128
     og.set_tuning(slots=best[3])
     return {"tuned_ms": best[0], "bucket": "%d/%d/%d" % bk, "wc_log2": best[1], "tile_kb": best[2],
             "slots": best[3]}
+
+
+def apply(report):
+    """Installs the result of an earlier tune_batch (its report dict): the
+    per-bucket table, the slots and the local-job threshold."""
+    clear()
+    table = {tuple(int(x) for x in k.split("/")): v for k, v in report.get("buckets", {}).items()}
+    set_table(table)
+    og.set_tuning(slots=int(report.get("slots") or 0), local_kb=int(report.get("local_kb") or 0))
