@@ -440,6 +440,20 @@ def percentiles(v):
             "requests": len(v)}
 
 
+def serve_native(shapes, seconds, think_us, temperature=50.0, lanes=4, max_batch=16, memory_mb=4096):
+    """The served annealing chains driven by the native client (serve_load):
+    one host thread per chain, no Python in the loop.  Returns its report;
+    it fails unless every chain's last served result equals its graph
+    evaluated alone."""
+    from odp_gb300 import build as b
+    chains = ["%d:%d:%d:%d" % (s["nodes"], s["degree"], s["seed"], s["proposal_seed"]) for s in shapes]
+    r = subprocess.run([b.SERVE_LOAD, "%g" % seconds, "%g" % think_us, str(lanes), str(max_batch), str(memory_mb),
+                        "%g" % temperature] + chains, capture_output=True, text=True, timeout=seconds + 300)
+    if r.returncode != 0:
+        raise RuntimeError("serve_load failed (%d): %s" % (r.returncode, r.stderr[-2000:]))
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
 def serving(seconds, rate=20000.0, saturate_seconds=4.0):
     """The served annealing workload; returns the report dict."""
     import odp_gb300 as og
@@ -490,8 +504,6 @@ def serving(seconds, rate=20000.0, saturate_seconds=4.0):
 
     wall, lat, lat_by_n = run(range(len(shapes)), seconds, len(shapes) / rate)
     st = srv.stats()
-    small = [k for k, s in enumerate(shapes) if s["nodes"] <= 8192]
-    sat_wall, sat_lat, sat_by_n = run(small, saturate_seconds, 0.0)
     # every chain's resident graph followed its client, and its served result
     # equals the same graph evaluated alone, bit for bit
     finals = [srv.wait(srv.submit(handles[k], undos[k])) for k in range(len(shapes))]
@@ -520,10 +532,22 @@ def serving(seconds, rate=20000.0, saturate_seconds=4.0):
         per_call_ms[n] = float(np.mean(ts)) * 1e3
 
     def same_mix(by_n):
-        cnt = sum(len(v) for v in by_n.values())
-        return cnt / sum(len(v) * per_call_ms[n] * 1e-3 for n, v in by_n.items())
+        """Evals/s of one ODP_Set_aspl call per request, for the same requests."""
+        cnt = sum(by_n.values())
+        return cnt / sum(k * per_call_ms[n] * 1e-3 for n, k in by_n.items())
 
-    done, sat_done = len(lat), len(sat_lat)
+    # the same chains from the native client: at the offered cap, and saturating with the n <= 8192 chains
+    native = serve_native(shapes, seconds, 1e6 * len(shapes) / rate)
+    small = [s for s in shapes if s["nodes"] <= 8192]
+    sat = serve_native(small, saturate_seconds, 0.0)
+    for rep in (native, sat):
+        rep["per_call_evals_per_s_same_mix"] = same_mix({int(k): v["requests"] for k, v in rep["by_n"].items()})
+        rep["served_over_per_call"] = rep["evals_per_s"] / rep["per_call_evals_per_s_same_mix"]
+    native["workload"] = "the 64 chains, native client (one host thread per chain), exponential think time for " \
+                         "a %d req/s offered cap" % int(rate)
+    sat["workload"] = "the %d chains with n <= 8192, native client, no think time" % len(small)
+
+    done = len(lat)
     return {"workload": "64 annealing chains, n in {1024,4096,16384,32768}, d in {8,16,24}, 2-opt proposals, "
                         "closed loop (1 outstanding per chain), exponential think time for a %d req/s offered cap"
                         % int(rate),
@@ -532,14 +556,12 @@ def serving(seconds, rate=20000.0, saturate_seconds=4.0):
             "latency_ms_by_n": {str(k): percentiles(v) for k, v in sorted(lat_by_n.items())},
             "evals_per_s_by_n": {str(k): len(v) / wall for k, v in sorted(lat_by_n.items())},
             "per_call_ms_by_n": {str(k): v for k, v in per_call_ms.items()},
-            "per_call_evals_per_s_same_mix": same_mix(lat_by_n),
+            "per_call_evals_per_s_same_mix": same_mix({n: len(v) for n, v in lat_by_n.items()}),
+            "client": "python threads (one per chain)",
             "batches": st["batches"], "mean_batch": st["batched_requests"] / max(1, st["batches"]),
             "max_batch": st["max_batch"], "max_concurrent_lanes": st["max_inflight_lanes"],
-            "saturating_small": {"workload": "the %d chains with n <= 8192, no think time" % len(small),
-                                 "seconds": sat_wall, "completed": sat_done, "evals_per_s": sat_done / sat_wall,
-                                 "latency_ms": percentiles(sat_lat),
-                                 "per_call_evals_per_s_same_mix": same_mix(sat_by_n),
-                                 "served_over_per_call": (sat_done / sat_wall) / same_mix(sat_by_n)},
+            "native_client": native,
+            "saturating_small": sat,
             "results_checked_alone_by_n": checked,
             "note": "the offered cap exceeds what any GPU can serve for n=32768 chains; chains are closed loop"}
 

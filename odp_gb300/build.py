@@ -3,7 +3,8 @@
     python -m odp_gb300.build            # or: python odp_gb300/build.py
 
 Outputs odp_gb300/libodp_gb300.so and odp_gb300/libodp_gb300.a; objects go to
-odp_gb300/_build/.  The CUDA translation unit is compiled with
+odp_gb300/_build/, with serve_load, a native client of the serving API that
+bench.py drives (linked against the shared library, not part of it).  The CUDA translation unit is compiled with
 `-gencode arch=compute_103a,code=sm_103a`; host C files with gcc.  The shared
 library links the CUDA runtime statically, so loading it needs only the
 driver (libcuda).
@@ -28,6 +29,8 @@ C_SOURCES = ["odp_graph.c", "odp_io.c", "odp_plan.c", "odp_aspl.c", "odp_batch.c
 
 SO_PATH = os.path.join(HERE, "libodp_gb300.so")
 A_PATH = os.path.join(HERE, "libodp_gb300.a")
+# a native client of the serving API that bench.py drives (not part of the library)
+SERVE_LOAD = os.path.join(BUILD, "serve_load")
 
 
 def _run(cmd):
@@ -67,6 +70,8 @@ def build(verbose_ptxas=False):
     if os.path.exists(A_PATH):
         os.remove(A_PATH)
     _run(["ar", "rcs", A_PATH] + objs)
+    _run(["gcc", "-O2", "-std=gnu11", "-Wall", "-I", INCLUDE, "-o", SERVE_LOAD, os.path.join(CSRC, "serve_load.c"),
+          "-L", HERE, "-lodp_gb300", "-Wl,-rpath,$ORIGIN/..", "-lpthread", "-lm"])
     if verbose_ptxas:
         sys.stdout.write("".join(logs))
     return SO_PATH

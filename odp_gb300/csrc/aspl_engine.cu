@@ -92,25 +92,47 @@ __device__ __forceinline__ int grid_base_row(int x, int height, int s)
 }
 
 /* Neighbour j of global vertex v of a rotation-symmetric grid
- * (utils_cuda.cu:25-59); -1 when the stored entry is out of range. */
-__device__ int grid_neighbour(const gbx_expand_desc &e, int v, int j)
+ * (utils_cuda.cu:25-59), read from the compact adjacency `adj`; -1 when the
+ * stored entry is out of range. */
+__device__ __forceinline__ int grid_source_row(const gbx_expand_desc &e, int v, int &back)
 {
-  const int w = e.width, h = e.height, s = e.s, d = e.d, n = e.n;
+  const int w = e.width, h = e.height, s = e.s;
   int x = v / h, y = v % h, bw = w / 2, bh = h / 2;
-  int src_row, back;
   if(s == 2){
-    if(x < bw){ src_row = v; back = 0; }
-    else      { src_row = grid_rotate(v, w, h, s, 180); back = 180; }
+    if(x < bw){ back = 0; return v; }
+    back = 180;
+    return grid_rotate(v, w, h, s, 180);
   }
-  else{
-    if(x < bw && y < bh)  { src_row = grid_base_row(v, h, s); back = 0; }
-    else if(x < bw)       { src_row = grid_base_row(grid_rotate(v, w, h, s, 270), h, s); back = 90; }
-    else if(y >= bh)      { src_row = grid_base_row(grid_rotate(v, w, h, s, 180), h, s); back = 180; }
-    else                  { src_row = grid_base_row(grid_rotate(v, w, h, s, 90), h, s); back = 270; }
-  }
-  int a = (e.adj_dev ? e.adj_dev : e.adj)[(size_t)src_row * d + j];
-  if(a < 0 || a >= n) return -1;
-  return back ? grid_rotate(a, w, h, s, back) : a;
+  if(x < bw && y < bh){ back = 0; return grid_base_row(v, h, s); }
+  if(x < bw)          { back = 90; return grid_base_row(grid_rotate(v, w, h, s, 270), h, s); }
+  if(y >= bh)         { back = 180; return grid_base_row(grid_rotate(v, w, h, s, 180), h, s); }
+  back = 270;
+  return grid_base_row(grid_rotate(v, w, h, s, 90), h, s);
+}
+
+/* Compact-adjacency position of entry j of global vertex v, and the
+ * rotation that maps the stored value back (grid symmetry) or the shift
+ * that does (general symmetry). */
+__device__ __forceinline__ size_t entry_source(const gbx_expand_desc &e, int v, int j, int &back)
+{
+  if(e.grid_s) return (size_t)grid_source_row(e, v, back) * e.d + j;
+  const int base = e.n / e.s;
+  back = (v / base) * base;
+  return (size_t)(v % base) * e.d + j;
+}
+
+/* Row-table entry from the stored value `a` of entry (v, j) (entries at or
+ * past the vertex's degree hold the row itself, and so does an out-of-range
+ * value, which also sets `bad`): the rotated vertex's row for symmetric
+ * grids, the shifted vertex (mod n) for general symmetry. */
+__device__ __forceinline__ int expand_value(const gbx_expand_desc &e, int a, int back, int j, int deg, int row,
+                                            bool &bad)
+{
+  if(j >= deg) return row;
+  if(a < 0 || a >= e.n){ bad = true; return row; }
+  if(e.grid_s) return e.itable[back ? grid_rotate(a, e.width, e.height, e.s, back) : a];
+  const int nb = a + back;
+  return nb >= e.n ? nb - e.n : nb;
 }
 
 /* One descriptor per blockIdx.y: its compact adjacency, read from host
@@ -146,33 +168,23 @@ __global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int nde
       if(descs[mid].first_vertex <= gv) lo = mid; else hi = mid - 1;
     }
     const gbx_expand_desc &e = descs[lo];
+    const int *adj = e.adj_dev ? e.adj_dev : e.adj;
     const int v = (int)(gv - e.first_vertex);
-    const int n = e.n, d = e.d, dp = e.dp;
+    const int d = e.d, dp = e.dp;
+    bool bad = false;
     int deg = e.ndeg ? e.ndeg[v] : d;
-    if(deg < 0 || deg > d){ atomicOr(err, GBX_ERR_BAD_ADJ); deg = deg < 0 ? 0 : d; }
+    if(deg < 0 || deg > d){ bad = true; deg = deg < 0 ? 0 : d; }
     const int row = e.grid_s ? e.itable[v] : v;
     int *out = e.nbr + (size_t)row * dp;
-    const int base = n / e.s;
-    const int m = v % base, shift = (v / base) * base;
     /* Entries that are not neighbours (beyond the vertex's degree, padding,
      * or out of range, which is also reported) hold the row itself: OR-ing a
      * row into itself changes nothing, so the gather needs no test. */
     for(int j = 0; j < dp; j++){
-      int nb = row;
-      if(j < deg){
-        if(e.grid_s){
-          int u = grid_neighbour(e, v, j);
-          if(u < 0) atomicOr(err, GBX_ERR_BAD_ADJ);
-          else nb = e.itable[u];
-        }
-        else{
-          int a = (e.adj_dev ? e.adj_dev : e.adj)[(size_t)m * d + j];
-          if(a < 0 || a >= n) atomicOr(err, GBX_ERR_BAD_ADJ);
-          else{ nb = a + shift; if(nb >= n) nb -= n; }
-        }
-      }
-      out[j] = nb;
+      int back = 0;
+      const int a = j < deg ? adj[entry_source(e, v, j, back)] : 0;
+      out[j] = expand_value(e, a, back, j, deg, row, bad);
     }
+    if(bad) atomicOr(err, GBX_ERR_BAD_ADJ);
   }
 }
 
@@ -713,39 +725,39 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
 }
 
 /* ---------------------------------------------------------------------- */
-/* Small graphs: one CTA per job, both bitset buffers and the neighbour     */
-/* table in shared memory, every level in the CTA.                           */
+/* Small graphs: one CTA per job, its neighbour table and both bitset        */
+/* buffers in shared memory, every level in the CTA.  The kernel reads the  */
+/* caller's compact adjacency from host memory itself and writes its        */
+/* outcome to pinned host memory, so a call is this one launch.             */
 /* ---------------------------------------------------------------------- */
 
 #define SMALL_THREADS 512
 #define SMALL_WARPS (SMALL_THREADS / 32)
+#define SMALL_LOADS 8            /* host loads in flight per thread while the table is built */
+
+struct SmallOutcome {
+  long long sum;
+  int level;
+  int stalled;
+};
 
 /* One job (chunk of sources) of a graph whose level fits in shared memory.
  * The same recurrence and bookkeeping as the engine: level 1 from the
  * neighbour lists, then P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]], the
  * bits set per level counted, the job complete when all n * nsrc bits are
- * set and stalled when a level adds none (or the level reaches n). */
+ * set and stalled when a level adds none (or the level reaches n).  Thread 0
+ * returns the job's share of the sum and its last level. */
 template <int WC, bool SP>
-__device__ void small_job(const gbx_job &jb, int job, unsigned char *smem, gbx_graph_acc *acc,
-                          gbx_job_out *job_out)
+__device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b1, SmallOutcome &out)
 {
   typedef RowShape<WC> S;
   constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;
   __shared__ unsigned long long s_cnt[2];
   __shared__ int s_go;
   const int n = jb.n, dp = jb.dp, d = jb.d, nsrc = jb.nsrc, src0 = jb.src0;
-  uint4 *b0 = reinterpret_cast<uint4 *>(smem);
-  uint4 *b1 = b0 + (size_t)n * S::VPR;
-  int *idx = reinterpret_cast<int *>(b1 + (size_t)n * S::VPR);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
-
-  const int4 *src = reinterpret_cast<const int4 *>(jb.nbr);
-  for(int i = threadIdx.x; i < (n * dp) >> 2; i += SMALL_THREADS) reinterpret_cast<int4 *>(idx)[i] = __ldg(src + i);
-  if(threadIdx.x == 0){
-    s_cnt[0] = s_cnt[1] = 0;
-    job_out[job].t_loaded = globaltimer();
-  }
+  if(threadIdx.x == 0) s_cnt[0] = s_cnt[1] = 0;
   __syncthreads();
 
   const unsigned long long full = (unsigned long long)n * (unsigned long long)nsrc;
@@ -803,12 +815,9 @@ __device__ void small_job(const gbx_job &jb, int job, unsigned char *smem, gbx_g
         go = 1;
       }
       else{
-        gbx_graph_acc *ga = &acc[jb.graph];
-        job_out[job].level = stalled ? -level : level;
-        job_out[job].t_done = globaltimer();
-        atomicAdd(&ga->sum, (unsigned long long)sum);
-        atomicMax(&ga->levels, level);
-        if(stalled) atomicOr(&ga->flags, 1);
+        out.sum = sum;
+        out.level = level;
+        out.stalled = stalled;
       }
       s_go = go;
     }
@@ -817,21 +826,79 @@ __device__ void small_job(const gbx_job &jb, int job, unsigned char *smem, gbx_g
   }
 }
 
+/* One CTA per job.  The job's graph descriptor and the caller's compact
+ * adjacency are read from host memory (pinned, or pageable where the device
+ * reads it through the host page tables); the row table is built straight
+ * into shared memory with the expansion rules of expand_kernel, eight
+ * independent host loads in flight per thread.  The job's record (level,
+ * error bits, sum, timestamps) goes to pinned host memory. */
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
-small_kernel(const gbx_job *__restrict__ jobs, gbx_graph_acc *acc, gbx_job_out *job_out)
+small_kernel(const gbx_job *__restrict__ jobs, const gbx_expand_desc *descs, gbx_small_rec *rec)
 {
   extern __shared__ __align__(16) unsigned char small_smem[];
+  __shared__ unsigned s_bad;
+  __shared__ gbx_expand_desc s_desc;
   const int job = blockIdx.x;
   const gbx_job jb = jobs[job];
+  unsigned long long t_loaded = 0;
+  if(threadIdx.x == 0){
+    t_loaded = globaltimer();
+    s_desc = descs[jb.graph];
+    s_bad = 0;
+  }
+  __syncthreads();
+  const gbx_expand_desc &e = s_desc;
+  const int n = jb.n, dp = jb.dp;
+  const size_t vecs = (size_t)n << (jb.wc_log2 - 1);              /* uint4 per bitset buffer */
+  uint4 *b0 = reinterpret_cast<uint4 *>(small_smem);
+  uint4 *b1 = b0 + vecs;
+  int *idx = reinterpret_cast<int *>(b1 + vecs);
+
+  bool bad = false;
+  const int total = n * dp;
+  for(int t0 = threadIdx.x; t0 < total; t0 += SMALL_THREADS * SMALL_LOADS){
+    int val[SMALL_LOADS], back[SMALL_LOADS];
+#pragma unroll
+    for(int k = 0; k < SMALL_LOADS; k++){
+      const int t = t0 + k * SMALL_THREADS;
+      const int v = t / dp, j = t - v * dp;
+      back[k] = 0;
+      val[k] = (t < total && j < e.d) ? e.adj[entry_source(e, v, j, back[k])] : 0;
+    }
+#pragma unroll
+    for(int k = 0; k < SMALL_LOADS; k++){
+      const int t = t0 + k * SMALL_THREADS;
+      if(t < total){
+        const int v = t / dp, j = t - v * dp;
+        int deg = e.ndeg ? e.ndeg[v] : e.d;
+        if(deg < 0 || deg > e.d){ bad = true; deg = deg < 0 ? 0 : e.d; }
+        const int row = e.grid_s ? e.itable[v] : v;
+        idx[row * dp + j] = expand_value(e, val[k], back[k], j, deg, row, bad);
+      }
+    }
+  }
+  if(bad) atomicOr(&s_bad, 1u);
+  __syncthreads();
+
+  SmallOutcome o = {0, 0, 0};
 #define ODP_SMALL_CASE(L) case L: \
-    if(jb.srcpos) small_job<(1 << L), true>(jb, job, small_smem, acc, job_out); \
-    else small_job<(1 << L), false>(jb, job, small_smem, acc, job_out); \
+    if(jb.srcpos) small_job<(1 << L), true>(jb, idx, b0, b1, o); \
+    else small_job<(1 << L), false>(jb, idx, b0, b1, o); \
     break;
   switch(jb.wc_log2){
     ODP_SMALL_CASE(1) ODP_SMALL_CASE(2) ODP_SMALL_CASE(3) ODP_SMALL_CASE(4)
     default: break;
   }
 #undef ODP_SMALL_CASE
+  if(threadIdx.x == 0){
+    gbx_small_rec r;
+    r.level = o.stalled ? -o.level : o.level;
+    r.err = s_bad ? GBX_ERR_BAD_ADJ : 0u;
+    r.sum = o.sum;
+    r.t_loaded = t_loaded;
+    r.t_done = globaltimer();
+    rec[job] = r;
+  }
 }
 
 /* L2 read ceiling for the roofline: every CTA streams an L2-resident buffer
@@ -988,13 +1055,18 @@ int gbx_small_prepare(void)
   return 0;
 }
 
-int gbx_small_launch(const gbx_job *d_jobs, int njobs, gbx_graph_acc *d_acc, gbx_job_out *d_job_out,
+int gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, gbx_small_rec *rec,
                      size_t smem_bytes, void *stream)
 {
   if(njobs <= 0) return 0;
   if(smem_bytes > GBX_SMALL_SMEM_MAX) return (int)cudaErrorInvalidValue;
-  small_kernel<<<njobs, SMALL_THREADS, smem_bytes, (cudaStream_t)stream>>>(d_jobs, d_acc, d_job_out);
+  small_kernel<<<njobs, SMALL_THREADS, smem_bytes, (cudaStream_t)stream>>>(d_jobs, descs, rec);
   return (int)cudaGetLastError();
+}
+
+int gbx_host_device_ptr(void *host, void **dev)
+{
+  return (int)cudaHostGetDevicePointer(dev, host, 0);
 }
 
 int gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream)
@@ -1159,8 +1231,8 @@ inline size_t up256(size_t x) { return (x + 255) & ~(size_t)255; }
 extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, const int *adjacency,
                                      int *diameter, long *sum, double *ASPL)
 {
-  if(nodes <= 0 || degree < 0 || symmetries <= 0 || nodes % symmetries != 0 || !adjacency || !diameter ||
-     !sum || !ASPL)
+  if(nodes <= 0 || degree < 0 || degree > GBX_MAX_DEGREE || symmetries <= 0 || nodes % symmetries != 0 ||
+     !adjacency || !diameter || !sum || !ASPL)
     return ODPX_ERR_INVALID;
   const int n = nodes, d = degree, s = symmetries, B = n / s, W = (B + 63) / 64;
   const int dp = ((d > 0 ? d : 1) + 3) & ~3;
@@ -1171,6 +1243,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   size_t off_adj = 0, off_nbr = 0, off_desc = 0, off_jobs = 0, off_state = 0, off_buf = 0, off_mask = 0, total = 0;
   size_t out_off = 0, acc_off = 0, levels_off = 0, state_bytes = 0;
   int wl = full_l2 < 6 ? full_l2 : 6, njobs = 0, nslots = 0, fits = 0;
+  const int mask_rows = (n + 63) & ~63;          /* each mask buffer starts on a 256-byte boundary */
   for(; wl >= 1; wl--){
     njobs = (W + (1 << wl) - 1) >> wl;
     if(njobs > NOALLOC_MAX_JOBS) break;
@@ -1186,7 +1259,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
     state_bytes = levels_off + sizeof(gbx_job_out) * (size_t)njobs;
     off_buf = up256(off_state + state_bytes);
     off_mask = up256(off_buf + sizeof(unsigned long long) * 2 * (size_t)nslots * ((size_t)n << wl));
-    total = off_mask + sizeof(unsigned) * 2 * (size_t)nslots * (size_t)n;
+    total = off_mask + sizeof(unsigned) * 2 * (size_t)nslots * (size_t)mask_rows;
     if(total <= ODPX_NOALLOC_SCRATCH_BYTES){ fits = 1; break; }
   }
   if(!fits){
@@ -1249,8 +1322,8 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
     sl[k].sum = ((long long)n * jobs[k].nsrc - jobs[k].nsrc) * s;
     sl[k].buf0 = bufs + (size_t)k * 2 * ((size_t)n << wl);
     sl[k].buf1 = sl[k].buf0 + ((size_t)n << wl);
-    sl[k].mask0 = (unsigned *)(base + off_mask) + (size_t)k * 2 * n;
-    sl[k].mask1 = sl[k].mask0 + n;
+    sl[k].mask0 = (unsigned *)(base + off_mask) + (size_t)k * 2 * mask_rows;
+    sl[k].mask1 = sl[k].mask0 + mask_rows;
   }
   ((gbx_ctrl *)(state + out_off))->next_job = (unsigned)nslots;
 

@@ -197,7 +197,7 @@ int ODPX_Batch_time_mode(ODPX_Batch *p, const int *const *adjacency, int repeats
   for(int r = 0; r < repeats && !rc; r++){
     if(fb) gbx_memset(g_flush, r & 0xff, fb, p->stream);
     gbx_event_record(ev[2 * r], p->stream);
-    if(mode == 0) rc = odp_plan_launch(p);
+    if(mode == 0 || p->small) rc = odp_plan_launch(p);   /* a small plan's call is its one kernel */
     else{
       if(gbx_memcpy_h2d(p->d_state, p->h_state_init, p->state_bytes, p->stream)) rc = ODPX_ERR_CUDA;
       else if(odp_plan_enqueue_engine(p)) rc = ODPX_ERR_CUDA;

@@ -47,6 +47,11 @@ typedef struct {
 
 #define GBX_JOB_ACTIVE 1
 
+/* Largest degree the engine takes: its row tables are staged in blocks of
+ * a few thousand neighbour entries that must hold several rows; rows are at
+ * most 512 entries (the degree rounded up to a multiple of 4). */
+#define GBX_MAX_DEGREE 508
+
 /* Shared memory a job of the small-graph kernel may use: its two bitset
  * buffers (2 x n x wc x 8 bytes) and its neighbour table (n x dp x 4). */
 #define GBX_SMALL_SMEM_MAX (200 * 1024)
@@ -141,11 +146,26 @@ int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int 
 /* Copies every descriptor's host array `adj` into its `adj_dev` with
  * coalesced 16-byte loads over the CPU-GPU link (pageable host memory). */
 int  gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream);
+/* Outcome of one job of the small-graph kernel, written to pinned host
+ * memory: its last level (negative: stalled), error bits (GBX_ERR_*), its
+ * share of the graph's ordered distance sum, and %globaltimer stamps. */
+typedef struct {
+  int level;
+  unsigned int err;
+  long long sum;
+  unsigned long long t_loaded, t_done;
+} gbx_small_rec;
+
 /* Jobs [0, njobs) of d_jobs, one CTA each, every level in shared memory
- * (smem_bytes per CTA, at most GBX_SMALL_SMEM_MAX); results go to the same
- * accumulators and per-job records as the engine's. */
-int  gbx_small_launch(const gbx_job *d_jobs, int njobs, gbx_graph_acc *d_acc, gbx_job_out *d_job_out,
+ * (smem_bytes per CTA, at most GBX_SMALL_SMEM_MAX).  Each CTA reads its
+ * graph's descriptor descs[job.graph] and the compact adjacency it names
+ * (`adj`) from host memory and builds the row table in shared memory; the
+ * job's record goes to rec[job].  `descs` and `rec` are device addresses of
+ * pinned host memory (gbx_host_device_ptr). */
+int  gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, gbx_small_rec *rec,
                       size_t smem_bytes, void *stream);
+/* Device address of pinned host memory. */
+int  gbx_host_device_ptr(void *host, void **dev);
 /* Allows the small-graph kernel GBX_SMALL_SMEM_MAX bytes of shared memory
  * (once per process; call before the first launch or capture). */
 int  gbx_small_prepare(void);

@@ -93,7 +93,7 @@ static int rows_per_pass(int wl)
 static int validate_shape(const odp_shape *sh)
 {
   int n = sh->grid ? sh->width * sh->height : sh->nodes;
-  if(n <= 0 || sh->degree < 0 || sh->symmetries <= 0) return ODPX_ERR_INVALID;
+  if(n <= 0 || sh->degree < 0 || sh->degree > GBX_MAX_DEGREE || sh->symmetries <= 0) return ODPX_ERR_INVALID;
   if(n % sh->symmetries != 0) return ODPX_ERR_INVALID;
   if(sh->grid && sh->symmetries != 1){
     int s = sh->symmetries, w = sh->width, h = sh->height;
@@ -434,7 +434,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
       tile_bytes = fill_tile;
       if(!tuning->local_kb_explicit && fill_tile < local_here) local_here = fill_tile;
     }
-    if(tuning->tile_rows > 0) g->tile_rows = tuning->tile_rows;
+    if(tuning->tile_rows > 0) g->tile_rows = ALIGN_UP(tuning->tile_rows, 4);   /* blocks start on 16-byte mask boundaries */
     else if(level_bytes <= local_here) g->tile_rows = g->n;
     else{
       double per_row = (double)wc * 8.0 * (g->d + 2);
@@ -525,8 +525,16 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   CK(gbx_malloc((void **)&p->d_jobs, sizeof(gbx_job) * (size_t)njobs));
   CK(gbx_malloc((void **)&p->d_state, p->state_bytes));
   p->direct = tuning->direct && gbx_pageable_access();
-  if(p->direct) CK(gbx_host_alloc((void **)&p->h_expand, sizeof(gbx_expand_desc) * (size_t)count));
-  else CK(gbx_host_alloc((void **)&p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4)));
+  /* Small plans read their descriptors (and through them the adjacency)
+   * from pinned host memory and write per-job records there. */
+  if(p->direct || small) CK(gbx_host_alloc((void **)&p->h_expand, sizeof(gbx_expand_desc) * (size_t)count));
+  if(!p->direct) CK(gbx_host_alloc((void **)&p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4)));
+  if(small){
+    CK(gbx_host_alloc((void **)&p->h_small_rec, sizeof(gbx_small_rec) * (size_t)njobs));
+    memset(p->h_small_rec, 0, sizeof(gbx_small_rec) * (size_t)njobs);
+    CK(gbx_host_device_ptr(p->h_small_rec, (void **)&p->d_small_rec));
+    CK(gbx_host_device_ptr(p->h_expand, (void **)&p->d_small_desc));
+  }
   CK(gbx_host_alloc((void **)&p->h_state_init, p->state_bytes));
   CK(gbx_host_alloc((void **)&p->h_state_out, p->out_bytes));
 
@@ -566,7 +574,16 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     if(h_nd) CK(gbx_memcpy_h2d(p->d_ndeg, h_nd, sizeof(int) * p->ndeg_ints, p->stream));
     if(h_it) CK(gbx_memcpy_h2d(p->d_itable, h_it, sizeof(int) * p->itable_ints, p->stream));
     CK(gbx_memcpy_h2d(p->d_expand, ed, sizeof(gbx_expand_desc) * (size_t)count, p->stream));
-    if(p->direct){
+    if(small){
+      /* the small-graph kernel reads `adj` itself: the caller's array (set
+       * per call) or this plan's pinned staging copy */
+      memcpy(p->h_expand, ed, sizeof(gbx_expand_desc) * (size_t)count);
+      for(int i = 0; i < count; i++){
+        p->h_expand[i].adj_dev = NULL;
+        p->h_expand[i].adj = p->direct ? NULL : p->h_adj + p->g[i].adj_off;
+      }
+    }
+    else if(p->direct){
       /* per call: `adj` names the caller's host array, `adj_dev` the device
        * copy that gbx_pull fills and expand reads */
       memcpy(p->h_expand, ed, sizeof(gbx_expand_desc) * (size_t)count);
@@ -593,16 +610,19 @@ void odp_plan_destroy(odp_plan *p)
   gbx_free(p->d_adj); gbx_free(p->d_ndeg); gbx_free(p->d_itable); gbx_free(p->d_nbr);
   gbx_free(p->d_slotbuf); gbx_free(p->d_slotmask); gbx_free(p->d_srcpos); gbx_free(p->d_expand); gbx_free(p->d_jobs); gbx_free(p->d_state);
   gbx_host_free(p->h_adj); gbx_host_free(p->h_expand); gbx_host_free(p->h_state_init); gbx_host_free(p->h_state_out);
+  gbx_host_free(p->h_small_rec);
   if(p->stream) gbx_stream_destroy(p->stream);
   free(p->h_jobs);
   free(p->g);
   free(p);
 }
 
-/* The per-call GPU work, in stream order. */
+/* The per-call GPU work, in stream order.  A small plan is one kernel: it
+ * reads the adjacency from host memory and writes its records there. */
 static int enqueue(odp_plan *p)
 {
   int e;
+  if(p->small) return odp_plan_enqueue_engine(p);
   if(p->direct){
     /* the descriptors carry this call's host pointers; the pull kernel copies
      * the arrays into the device copy that expand reads */
@@ -622,8 +642,7 @@ static int enqueue(odp_plan *p)
 int odp_plan_enqueue_engine(odp_plan *p)
 {
   if(p->small)
-    return gbx_small_launch(p->d_jobs, p->njobs, (gbx_graph_acc *)(p->d_state + p->acc_off),
-                            (gbx_job_out *)(p->d_state + p->levels_off), p->small_smem, p->stream);
+    return gbx_small_launch(p->d_jobs, p->njobs, p->d_small_desc, p->d_small_rec, p->small_smem, p->stream);
   return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
                            (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),
                            (gbx_job_out *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->any_active,
@@ -754,9 +773,52 @@ static int reorder_by_duration(odp_plan *p)
   return 0;
 }
 
+/* Small plans: the per-job records folded per graph, as the engine's
+ * accumulators fold them (sum of the jobs' sums, the largest level, stalled
+ * if any job stalled); the levels and stamps also go to the per-job outcome
+ * table that the introspection calls read. */
+static int finish_small(odp_plan *p, odp_result *results)
+{
+  gbx_job_out *jo = (gbx_job_out *)(p->h_state_out + (p->levels_off - p->out_off));
+  unsigned int err = 0;
+  for(int k = 0; k < p->njobs; k++){
+    err |= p->h_small_rec[k].err;
+    jo[k].level = p->h_small_rec[k].level;
+    jo[k].t_loaded = p->h_small_rec[k].t_loaded;
+    jo[k].t_done = p->h_small_rec[k].t_done;
+  }
+  if(err & GBX_ERR_BAD_ADJ) return ODPX_ERR_ADJACENCY;
+  for(int i = 0; i < p->ngraphs; i++){
+    unsigned long long sum = 0;
+    int level = 0, stalled = 0;
+    for(int k = 0; k < p->njobs; k++){
+      const gbx_small_rec *r = &p->h_small_rec[k];
+      if(p->h_jobs[k].graph != i) continue;
+      sum += (unsigned long long)r->sum;
+      const int l = r->level < 0 ? -r->level : r->level;
+      if(l > level) level = l;
+      if(r->level < 0) stalled = 1;
+    }
+    const odp_plan_graph *g = &p->g[i];
+    odp_result *res = &results[i];
+    if(stalled){
+      res->diameter = INT_MAX;
+      res->sum = LONG_MAX;
+      res->aspl = DBL_MAX;
+      continue;
+    }
+    long total = (long)sum;
+    res->diameter = level;
+    res->aspl = total / (((double)g->n - 1) * g->n);
+    res->sum = (long)(total / 2.0);
+  }
+  return 0;
+}
+
 int odp_plan_finish(odp_plan *p, odp_result *results)
 {
   if(gbx_stream_sync(p->stream)) return ODPX_ERR_CUDA;
+  if(p->small) return finish_small(p, results);
   const gbx_ctrl *ctrl = (const gbx_ctrl *)p->h_state_out;
   unsigned int err = *(const unsigned int *)(p->h_state_out + sizeof(gbx_ctrl)) | ctrl->error;
   if(err & GBX_ERR_TIMEOUT) return ODPX_ERR_TIMEOUT;
@@ -800,6 +862,11 @@ unsigned long long odp_plan_tiles(const odp_plan *p)
 
 unsigned int odp_plan_error(const odp_plan *p)
 {
+  if(p->small){
+    unsigned int err = 0;
+    for(int k = 0; k < p->njobs; k++) err |= p->h_small_rec[k].err;
+    return err;
+  }
   const gbx_ctrl *ctrl = (const gbx_ctrl *)p->h_state_out;
   return *(const unsigned int *)(p->h_state_out + sizeof(gbx_ctrl)) | ctrl->error;
 }

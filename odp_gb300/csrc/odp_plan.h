@@ -74,6 +74,9 @@ typedef struct odp_plan {
   gbx_expand_desc *h_expand;   /* pinned copy of the expand descriptors (direct plans) */
   int small;                   /* every job runs in the small-graph kernel, in shared memory */
   size_t small_smem;           /* shared memory per CTA of the small-graph kernel */
+  gbx_small_rec *h_small_rec;  /* small plans: per-job records, pinned; the kernel writes them */
+  gbx_small_rec *d_small_rec;  /*   the same memory, as the device addresses it */
+  gbx_expand_desc *d_small_desc; /* small plans: h_expand as the device addresses it */
 } odp_plan;
 
 typedef struct {

@@ -430,7 +430,7 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
   if(!s || !gr || !gr->adjacency || !handle) return ODPX_ERR_INVALID;
   int n = gr->grid ? gr->width * gr->height : gr->nodes;
   int sym = gr->symmetries;
-  if(n <= 0 || sym <= 0 || n % sym || gr->degree < 1) return ODPX_ERR_INVALID;
+  if(n <= 0 || sym <= 0 || n % sym || gr->degree < 1 || gr->degree > GBX_MAX_DEGREE) return ODPX_ERR_INVALID;
   int grid_s = gr->grid && sym != 1;
   if(grid_s && (sym != 2 && sym != 4)) grid_s = 0;           /* the general rule, as ODP_Init_aspl_grid_s */
   if(grid_s && ((gr->width % 2) || (sym == 4 && (gr->height % 2 || gr->width != gr->height)))) return ODPX_ERR_INVALID;
