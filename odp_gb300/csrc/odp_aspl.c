@@ -113,7 +113,9 @@ static void init_common(const odp_shape *sh)
   odp_tuning t;
   odp_tuning_for(1, &t);
   int rc = odp_plan_create(sh, 1, &t, &S.plan);
-  if(rc == ODPX_ERR_INVALID) fail("Invalid graph parameters (nodes=%d, symmetries=%d)\n", nodes, sh->symmetries);
+  if(rc == ODPX_ERR_INVALID)
+    fail("Invalid graph parameters (nodes=%d, degree=%d, symmetries=%d; the degree may be at most %d)\n", nodes,
+         sh->degree, sh->symmetries, GBX_MAX_DEGREE);
   if(rc) fail("GPU initialisation failed (error %d)\n", rc);
   S.initialized = 1;
 }

@@ -53,3 +53,23 @@ def test_invalid_batch_shapes_are_refused_before_the_device():
             assert e.code == og.ERR_INVALID, (kw, e.code)
         else:
             raise AssertionError("accepted: %s" % kw)
+
+
+def test_degrees_above_the_engine_limit_are_refused():
+    """The engine stages neighbour lists of at most 512 entries per row: a
+    degree above 508 is refused by the batch API (ODPX_ERR_INVALID) and by
+    the drop-in, which exits with a message naming the limit."""
+    import subprocess
+    import sys
+    import numpy as np
+    import odp_gb300 as og
+    adj = np.zeros((16, 600), dtype=np.int32)
+    try:
+        og.Batch([og.GraphSpec(adj, nodes=16)])
+    except og.ODPError as e:
+        assert e.code == og.ERR_INVALID
+    else:
+        raise AssertionError("degree 600 accepted")
+    code = "import sys; sys.path.insert(0, %r); import odp_gb300 as og; og.init_aspl_general(1024, 600)" % ROOT
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 1 and "at most 508" in r.stderr, (r.returncode, r.stderr)
