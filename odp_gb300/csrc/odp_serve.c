@@ -55,22 +55,30 @@ typedef struct {
   int rc, diameter;
   long sum;
   double aspl;
+  pthread_cond_t *waiter;      /* the condition the one thread waiting for it sleeps on, or NULL */
 } serve_req;
 
+/* A lane's per-batch state block, laid out anew for every batch so that one
+ * small copy carries all of it: control block and error word | per-graph
+ * accumulators | the active slots | the jobs | per-job outcomes (device
+ * only).  The host copy is pinned; the device reads the batch's writes
+ * (delta updates) straight from pinned memory. */
+#define LANE_ACC_OFF 128       /* after gbx_ctrl (64 B) and the error word */
 typedef struct {
   void *stream, *ev;
   int busy, nslots, max_jobs, max_batch, max_writes, blocks;
-  size_t slot_words, slot_rows, out_off, acc_off, levels_off, state_bytes;
+  size_t slot_words, slot_rows, block_bytes;
   unsigned long long *d_slotbuf;
   unsigned *d_slotmask;
-  char *d_state;
-  gbx_job *d_jobs;
-  gbx_write *d_writes;
-  char *h_state, *h_out;
-  gbx_job *h_jobs;
-  gbx_write *h_writes;
+  char *d_block, *h_block;     /* the state block, device and pinned host */
+  char *h_out;                 /* pinned: control block and accumulators of the finished batch */
+  gbx_write *h_writes, *dh_writes; /* pinned writes of the batch, and their device address */
+  gbx_job *h_jobs;             /* jobs as they are formed (host) */
   long long *members;          /* request ids of the running batch */
   int nmembers;
+  /* the batch formed and not yet issued */
+  int b_nw, b_njobs, b_nslots;
+  size_t b_slots_off, b_jobs_off, b_outcomes_off, b_acc_bytes;
 } serve_lane;
 
 typedef struct odp_server odp_server;
@@ -79,7 +87,8 @@ struct odp_server {
   ODPX_Serve_config cfg;
   pthread_t thread;
   pthread_mutex_t mu;
-  pthread_cond_t cv_work, cv_done;
+  pthread_cond_t cv_work, cv_done;   /* cv_done: the shared wake-up of shared_waiters */
+  int shared_waiters;          /* threads sleeping on cv_done */
   int stop, started;
   void *ctl_stream;
   serve_graph *graphs;
@@ -120,8 +129,9 @@ static int rotate(int v, int width, int height, int s, int deg)   /* ODP_ROTATE,
 static void lane_free(serve_lane *l)
 {
   if(l->stream) gbx_stream_sync(l->stream);
-  gbx_free(l->d_slotbuf); gbx_free(l->d_slotmask); gbx_free(l->d_state); gbx_free(l->d_jobs); gbx_free(l->d_writes);
-  gbx_host_free(l->h_state); gbx_host_free(l->h_out); gbx_host_free(l->h_jobs); gbx_host_free(l->h_writes);
+  gbx_free(l->d_slotbuf); gbx_free(l->d_slotmask); gbx_free(l->d_block);
+  gbx_host_free(l->h_block); gbx_host_free(l->h_out); gbx_host_free(l->h_writes);
+  free(l->h_jobs);
   if(l->ev) gbx_event_destroy(l->ev);
   if(l->stream) gbx_stream_destroy(l->stream);
   free(l->members);
@@ -137,22 +147,20 @@ static int lane_init(serve_lane *l, const ODPX_Serve_config *c, int nslots, int 
   l->max_writes = c->max_batch * 4096;
   l->slot_words = ALIGN_UP((size_t)c->max_nodes << c->wc_log2, 32);
   l->slot_rows = ALIGN_UP((size_t)c->max_nodes, 64);
-  l->out_off = sizeof(gbx_slot) * (size_t)nslots;
-  l->acc_off = l->out_off + sizeof(gbx_ctrl) + 64;
-  l->levels_off = l->acc_off + ALIGN_UP(sizeof(gbx_graph_acc) * (size_t)l->max_batch, 64);
-  l->state_bytes = l->levels_off + ALIGN_UP(sizeof(gbx_job_out) * (size_t)l->max_jobs, 64);
-  if(gbx_stream_create(&l->stream) || gbx_event_create(&l->ev) ||
+  l->block_bytes = LANE_ACC_OFF + ALIGN_UP(sizeof(gbx_graph_acc) * (size_t)l->max_batch, 256) +
+                   sizeof(gbx_slot) * (size_t)nslots + sizeof(gbx_job) * (size_t)l->max_jobs +
+                   ALIGN_UP(sizeof(gbx_job_out) * (size_t)l->max_jobs, 64);
+  l->h_jobs = malloc(sizeof(gbx_job) * (size_t)l->max_jobs);
+  l->members = malloc(sizeof(long long) * (size_t)l->max_batch);
+  if(!l->h_jobs || !l->members || gbx_stream_create(&l->stream) || gbx_event_create(&l->ev) ||
      gbx_malloc((void **)&l->d_slotbuf, sizeof(unsigned long long) * l->slot_words * 2 * (size_t)nslots) ||
      gbx_malloc((void **)&l->d_slotmask, sizeof(unsigned) * l->slot_rows * 2 * (size_t)nslots) ||
-     gbx_malloc((void **)&l->d_state, l->state_bytes) ||
-     gbx_malloc((void **)&l->d_jobs, sizeof(gbx_job) * (size_t)l->max_jobs) ||
-     gbx_malloc((void **)&l->d_writes, sizeof(gbx_write) * (size_t)l->max_writes) ||
-     gbx_host_alloc((void **)&l->h_state, l->state_bytes) ||
-     gbx_host_alloc((void **)&l->h_out, l->state_bytes - l->out_off) ||
-     gbx_host_alloc((void **)&l->h_jobs, sizeof(gbx_job) * (size_t)l->max_jobs) ||
-     gbx_host_alloc((void **)&l->h_writes, sizeof(gbx_write) * (size_t)l->max_writes))
+     gbx_malloc((void **)&l->d_block, l->block_bytes) ||
+     gbx_host_alloc((void **)&l->h_block, l->block_bytes) ||
+     gbx_host_alloc((void **)&l->h_out, LANE_ACC_OFF + sizeof(gbx_graph_acc) * (size_t)l->max_batch) ||
+     gbx_host_alloc((void **)&l->h_writes, sizeof(gbx_write) * (size_t)l->max_writes) ||
+     gbx_host_device_ptr(l->h_writes, (void **)&l->dh_writes))
     return ODPX_ERR_CUDA;
-  l->members = malloc(sizeof(long long) * (size_t)l->max_batch);
   return 0;
 }
 
@@ -189,11 +197,13 @@ static int delta_writes(serve_graph *g, const ODPX_Delta *dl, gbx_write *w)
   return k;
 }
 
+/* Results of lane l's finished batch go to its requests, and each request's
+ * waiting thread, if any, is woken.  Called with the mutex held. */
 static void finish_batch(odp_server *s, serve_lane *l)
 {
   const gbx_ctrl *ctrl = (const gbx_ctrl *)l->h_out;
   unsigned err = *(const unsigned *)(l->h_out + sizeof(gbx_ctrl)) | ctrl->error;
-  const gbx_graph_acc *acc = (const gbx_graph_acc *)(l->h_out + (l->acc_off - l->out_off));
+  const gbx_graph_acc *acc = (const gbx_graph_acc *)(l->h_out + LANE_ACC_OFF);
   double t = now_s();
   for(int i = 0; i < l->nmembers; i++){
     serve_req *r = &s->reqs[l->members[i]];
@@ -209,15 +219,17 @@ static void finish_batch(odp_server *s, serve_lane *l)
     r->t_done = t;
     r->state = 2;
     g->busy = 0;
+    if(r->waiter) pthread_cond_signal(r->waiter);
   }
   s->stats.requests_done += l->nmembers;
   l->busy = 0;
   l->nmembers = 0;
 }
 
-/* Forms a batch from the oldest pending requests whose graphs are idle and
- * launches it on lane l.  Called with the mutex held. */
-static int launch_batch(odp_server *s, serve_lane *l, double max_seed_cost)
+/* Forms a batch from the oldest pending requests whose graphs are idle on
+ * lane l: its writes, jobs and state block, ready for issue_batch.  Called
+ * with the mutex held; returns the number of requests taken. */
+static int form_batch(odp_server *s, serve_lane *l, double max_seed_cost)
 {
   int nreq = 0, njobs = 0, nw = 0;
   double seed_cost = 0;
@@ -265,8 +277,12 @@ static int launch_batch(odp_server *s, serve_lane *l, double max_seed_cost)
     fp += f;
     nslots++;
   }
-  memset(l->h_state, 0, l->state_bytes);
-  gbx_slot *sl = (gbx_slot *)l->h_state;
+  l->b_acc_bytes = sizeof(gbx_graph_acc) * (size_t)nreq;
+  l->b_slots_off = LANE_ACC_OFF + ALIGN_UP(l->b_acc_bytes, 256);
+  l->b_jobs_off = l->b_slots_off + sizeof(gbx_slot) * (size_t)nslots;
+  l->b_outcomes_off = ALIGN_UP(l->b_jobs_off + sizeof(gbx_job) * (size_t)njobs, 64);
+  memset(l->h_block, 0, l->b_jobs_off);
+  gbx_slot *sl = (gbx_slot *)(l->h_block + l->b_slots_off);
   for(int k = 0; k < nslots; k++){
     const gbx_job *j = &l->h_jobs[k];
     sl[k].ticket = (unsigned long long)j->ntiles << 32;
@@ -280,74 +296,100 @@ static int launch_batch(odp_server *s, serve_lane *l, double max_seed_cost)
     sl[k].mask0 = l->d_slotmask + (size_t)k * 2 * l->slot_rows;
     sl[k].mask1 = sl[k].mask0 + l->slot_rows;
   }
-  ((gbx_ctrl *)(l->h_state + l->out_off))->next_job = (unsigned)nslots;
-  /* slots past nslots stay empty (ticket 0); the engine retires them */
-  size_t out_bytes = l->levels_off + sizeof(gbx_job_out) * (size_t)njobs - l->out_off;
-  int e = 0;
-  if(nw) e |= gbx_memcpy_h2d(l->d_writes, l->h_writes, sizeof(gbx_write) * (size_t)nw, l->stream);
-  if(nw) e |= gbx_scatter(l->d_writes, nw, l->stream);
-  e |= gbx_memcpy_h2d(l->d_jobs, l->h_jobs, sizeof(gbx_job) * (size_t)njobs, l->stream);
-  e |= gbx_memcpy_h2d(l->d_state, l->h_state, l->levels_off, l->stream);
-  e |= gbx_engine_launch(l->d_jobs, njobs, (gbx_slot *)l->d_state, nslots, (gbx_ctrl *)(l->d_state + l->out_off),
-                         (gbx_graph_acc *)(l->d_state + l->acc_off), (gbx_job_out *)(l->d_state + l->levels_off),
-                         60ull * 1000000000ull, l->blocks, 0, l->stream);
-  e |= gbx_memcpy_d2h(l->h_out, l->d_state + l->out_off, out_bytes, l->stream);
-  e |= gbx_event_record(l->ev, l->stream);
+  memcpy(l->h_block + l->b_jobs_off, l->h_jobs, sizeof(gbx_job) * (size_t)njobs);
+  ((gbx_ctrl *)l->h_block)->next_job = (unsigned)nslots;
+  l->b_nw = nw;
+  l->b_njobs = njobs;
+  l->b_nslots = nslots;
   l->nmembers = nreq;
   l->busy = 1;
   s->stats.batches++;
   s->stats.batched_requests += nreq;
   if(nreq > s->stats.max_batch) s->stats.max_batch = nreq;
-  if(e){
-    for(int i = 0; i < nreq; i++){
-      serve_req *r = &s->reqs[l->members[i]];
-      r->rc = ODPX_ERR_CUDA; r->state = 2; r->t_done = now_s();
-      s->graphs[r->graph].busy = 0;
-    }
-    l->busy = 0;
-    l->nmembers = 0;
-    return -1;
-  }
   return nreq;
 }
 
+/* Issues lane l's formed batch on its stream: the delta writes (read by the
+ * scatter kernel from pinned memory), one copy of the state block, the
+ * engine, one copy back of the control block and accumulators, and the
+ * completion event.  Touches only the lane, so it runs without the mutex. */
+static int issue_batch(serve_lane *l)
+{
+  int e = 0;
+  if(l->b_nw) e |= gbx_scatter(l->dh_writes, l->b_nw, l->stream);
+  e |= gbx_memcpy_h2d(l->d_block, l->h_block, l->b_outcomes_off, l->stream);
+  e |= gbx_engine_launch((const gbx_job *)(l->d_block + l->b_jobs_off), l->b_njobs,
+                         (gbx_slot *)(l->d_block + l->b_slots_off), l->b_nslots, (gbx_ctrl *)l->d_block,
+                         (gbx_graph_acc *)(l->d_block + LANE_ACC_OFF),
+                         (gbx_job_out *)(l->d_block + l->b_outcomes_off), 60ull * 1000000000ull, l->blocks, 0,
+                         l->stream);
+  e |= gbx_memcpy_d2h(l->h_out, l->d_block, LANE_ACC_OFF + l->b_acc_bytes, l->stream);
+  e |= gbx_event_record(l->ev, l->stream);
+  return e;
+}
+
+/* A batch that could not be issued fails its requests.  Mutex held. */
+static void fail_batch(odp_server *s, serve_lane *l)
+{
+  for(int i = 0; i < l->nmembers; i++){
+    serve_req *r = &s->reqs[l->members[i]];
+    r->rc = ODPX_ERR_CUDA; r->state = 2; r->t_done = now_s();
+    s->graphs[r->graph].busy = 0;
+    if(r->waiter) pthread_cond_signal(r->waiter);
+  }
+  l->busy = 0;
+  l->nmembers = 0;
+}
+
+/* The scheduler thread.  Lanes belong to it alone: their CUDA calls (event
+ * queries, copies, launches) run with the mutex released, so clients that
+ * submit or wait are not held up by them; requests and graphs are touched
+ * only with the mutex held. */
+#define MAX_LANES 64
 static void *scheduler(void *arg)
 {
   odp_server *s = arg;
   /* the completion polling sleeps for microseconds: keep the kernel from
    * stretching them by its default 50 us timer slack */
   prctl(PR_SET_TIMERSLACK, 1UL, 0, 0, 0);
+  const int nl = s->cfg.lanes < MAX_LANES ? s->cfg.lanes : MAX_LANES;
+  int q[MAX_LANES];
+  serve_lane *formed[MAX_LANES];
   pthread_mutex_lock(&s->mu);
   while(!s->stop){
-    int busy = 0, progress = 0;
-    for(int i = 0; i < s->cfg.lanes; i++){
-      serve_lane *l = &s->lanes[i];
-      if(l->busy){
-        int q = gbx_event_query(l->ev);
-        if(q == 0){ finish_batch(s, l); progress = 1; }
-        else if(q != 1){                             /* a CUDA error: fail the batch */
-          gbx_stream_sync(l->stream);
-          finish_batch(s, l);
-          progress = 1;
-        }
-      }
-    }
-    if(progress) pthread_cond_broadcast(&s->cv_done);
-    int have_pending = s->next_pending < s->nreqs;
+    int progress = 0;
+    /* completions: queried without the mutex */
+    pthread_mutex_unlock(&s->mu);
+    for(int i = 0; i < nl; i++) q[i] = s->lanes[i].busy ? gbx_event_query(s->lanes[i].ev) : 1;
+    for(int i = 0; i < nl; i++)
+      if(s->lanes[i].busy && q[i] != 0 && q[i] != 1) gbx_stream_sync(s->lanes[i].stream);  /* a CUDA error */
+    pthread_mutex_lock(&s->mu);
+    for(int i = 0; i < nl; i++)
+      if(s->lanes[i].busy && q[i] != 1){ finish_batch(s, &s->lanes[i]); progress = 1; }
+    if(progress && s->shared_waiters) pthread_cond_broadcast(&s->cv_done);
     /* With several lanes, lane 0 takes only the cheaper half of the cost
      * range (below the geometric mean of the registered graphs' costs), so
      * small requests always find a lane that large batches cannot hold. */
-    const double small = s->cfg.lanes > 1 ? sqrt(s->min_cost * s->max_cost) : HUGE_VAL;
-    for(int i = 0; i < s->cfg.lanes && have_pending; i++){
+    const double small = nl > 1 ? sqrt(s->min_cost * s->max_cost) : HUGE_VAL;
+    int nformed = 0;
+    for(int i = 0; i < nl && s->next_pending < s->nreqs; i++){
       serve_lane *l = &s->lanes[i];
-      if(!l->busy && launch_batch(s, l, i == 0 ? small : HUGE_VAL) > 0) progress = 1;
-      have_pending = s->next_pending < s->nreqs;
+      if(!l->busy && form_batch(s, l, i == 0 ? small : HUGE_VAL) > 0) formed[nformed++] = l;
+    }
+    if(nformed){
+      /* issued without the mutex; failures are handed back with it */
+      pthread_mutex_unlock(&s->mu);
+      int failed[MAX_LANES];
+      for(int k = 0; k < nformed; k++) failed[k] = issue_batch(formed[k]) != 0;
+      pthread_mutex_lock(&s->mu);
+      for(int k = 0; k < nformed; k++) if(failed[k]) fail_batch(s, formed[k]);
+      progress = 1;
     }
     int inflight = 0;
-    for(int i = 0; i < s->cfg.lanes; i++) inflight += s->lanes[i].busy;
-    busy = inflight > 0;
+    for(int i = 0; i < nl; i++) inflight += s->lanes[i].busy;
     if(inflight > s->stats.max_inflight_lanes) s->stats.max_inflight_lanes = inflight;
-    if(!busy && !have_pending){
+    const int have_pending = s->next_pending < s->nreqs;
+    if(!inflight && !have_pending){
       pthread_cond_wait(&s->cv_work, &s->mu);
     }
     else if(!progress){
@@ -601,7 +643,23 @@ int ODPX_Serve_wait(ODPX_Server *s, long long request, int *diameter, long *sum,
   if(!s) return ODPX_ERR_INVALID;
   pthread_mutex_lock(&s->mu);
   if(request < 0 || request >= s->nreqs){ pthread_mutex_unlock(&s->mu); return ODPX_ERR_INVALID; }
-  while(s->reqs[request].state != 2) pthread_cond_wait(&s->cv_done, &s->mu);
+  /* the thread that waits for a request sleeps on a condition of its own,
+   * which only that request's completion signals; a second thread waiting
+   * for the same request uses the shared one */
+  pthread_cond_t cv;
+  int own = s->reqs[request].waiter == NULL && s->reqs[request].state != 2;
+  if(own){
+    pthread_cond_init(&cv, NULL);
+    s->reqs[request].waiter = &cv;
+    while(s->reqs[request].state != 2) pthread_cond_wait(&cv, &s->mu);
+    s->reqs[request].waiter = NULL;
+    pthread_cond_destroy(&cv);
+  }
+  else{
+    s->shared_waiters++;
+    while(s->reqs[request].state != 2) pthread_cond_wait(&s->cv_done, &s->mu);
+    s->shared_waiters--;
+  }
   serve_req *r = &s->reqs[request];
   copy_result(r, diameter, sum, ASPL, latency_s);
   int rc = r->rc;
@@ -639,7 +697,9 @@ int ODPX_Serve_adjacency(ODPX_Server *s, int handle, int *adjacency)
   pthread_mutex_lock(&s->mu);
   if(handle < 0 || handle >= s->ngraphs){ pthread_mutex_unlock(&s->mu); return ODPX_ERR_INVALID; }
   serve_graph *g = &s->graphs[handle];
+  s->shared_waiters++;
   while(g->busy) pthread_cond_wait(&s->cv_done, &s->mu);
+  s->shared_waiters--;
   /* also wait until no pending request carries deltas for it */
   size_t bytes = sizeof(int) * (size_t)g->B * g->d;
   int e = gbx_memcpy_d2h(adjacency, g->d_adj, bytes, s->ctl_stream) | gbx_stream_sync(s->ctl_stream);
