@@ -622,8 +622,20 @@ def anneal(seconds, temperature=50.0):
             "accepted": accepted}
 
 
+def pin_local_gpu(local):
+    """Under torchrun every rank evaluates on its own GPU: CUDA_VISIBLE_DEVICES
+    is narrowed to the rank's local device before anything initialises CUDA
+    in this process.  Returns the device's index for nvidia-smi."""
+    visible = os.environ.get("CUDA_VISIBLE_DEVICES")
+    devices = [d for d in visible.split(",") if d.strip()] if visible else None
+    dev = devices[local % len(devices)].strip() if devices else str(local)
+    os.environ["CUDA_VISIBLE_DEVICES"] = dev
+    return int(dev) if dev.isdigit() else local
+
+
 def run_own(args):
     rank, world, local = dist_info()
+    smi_index = pin_local_gpu(local) if world > 1 else local
     dist = Dist(world)
     import odp_gb300 as og
     import baseline
@@ -657,7 +669,7 @@ def run_own(args):
     for _ in range(args.warmup):
         batch.time(1, mode=1, flush_mb=args.flush_mb)
     dist.barrier()
-    with ClockSampler(local) as clk:
+    with ClockSampler(smi_index) as clk:
         ms = batch.time(args.steps, mode=1, flush_mb=args.flush_mb)
     ms = dist.max(ms)
     dist.barrier()

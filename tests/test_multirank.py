@@ -86,3 +86,13 @@ def test_reference_arm_json_line_carries_the_contract_keys():
     e = rec["e2e"]
     assert e["value"] == rec["value"] and e["unit"] == rec["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+
+
+def test_each_rank_is_pinned_to_its_local_gpu(monkeypatch):
+    """Under torchrun the GPU arm narrows CUDA_VISIBLE_DEVICES to the rank's
+    local device (the n-th of the visible ones) before CUDA starts."""
+    import bench
+    monkeypatch.setenv("CUDA_VISIBLE_DEVICES", "4,5,6,7")
+    assert bench.pin_local_gpu(1) == 5 and os.environ["CUDA_VISIBLE_DEVICES"] == "5"
+    monkeypatch.delenv("CUDA_VISIBLE_DEVICES")
+    assert bench.pin_local_gpu(2) == 2 and os.environ["CUDA_VISIBLE_DEVICES"] == "2"
