@@ -486,9 +486,21 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
     if(level > 1 && (jb.flags & GBX_JOB_ACTIVE)){
       for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS) st.own[r] = __ldcg(Mprev + b0 + r);
       __syncthreads();
-      for(int i = threadIdx.x; i < nr * dp; i += ENGINE_THREADS){
-        const int q = st.idx[i];
-        st.nmask[i] = q >= 0 ? __ldcg(Mprev + q) : 0u;
+      /* the neighbours' masks: eight independent gathers in flight per thread */
+      const int total = nr * dp;
+      for(int i0 = threadIdx.x; i0 < total; i0 += ENGINE_THREADS * 8){
+        unsigned v[8];
+#pragma unroll
+        for(int k = 0; k < 8; k++){
+          const int i = i0 + k * ENGINE_THREADS;
+          const int q = i < total ? st.idx[i] : -1;
+          v[k] = q >= 0 ? __ldcg(Mprev + q) : 0u;
+        }
+#pragma unroll
+        for(int k = 0; k < 8; k++){
+          const int i = i0 + k * ENGINE_THREADS;
+          if(i < total) st.nmask[i] = v[k];
+        }
       }
       __syncthreads();
       for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS){

@@ -180,3 +180,22 @@ def test_served_results_at_the_served_sizes():
             if n >= 16384 and step in (3, steps - 1):
                 assert same(got, oracle.aspl(host, nodes=n)), (n, d, step)
         b.close()
+
+
+def test_native_client_chains_match_their_graphs_alone():
+    """serve_load (the native client bench.py drives): 12 chains of three
+    sizes, one host thread each, first without think time and then with it;
+    every chain's last served result must equal its graph evaluated alone
+    (the program checks and exits non-zero otherwise)."""
+    import json
+    import subprocess
+    from odp_gb300 import build as b
+    chains = ["%d:%d:%d:%d" % (n, d, 3000 + i, 4000 + i)
+              for i, (n, d) in enumerate([(1024, 8), (2048, 12), (4096, 16)] * 4)]
+    for think_us in ("0", "200"):
+        r = subprocess.run([b.SERVE_LOAD, "1.0", think_us, "4", "16", "1024", "50"] + chains, capture_output=True,
+                           text=True, timeout=240)
+        assert r.returncode == 0, r.stderr[-2000:]
+        rep = json.loads(r.stdout.strip().splitlines()[-1])
+        assert rep["checked"] == len(chains) and rep["mismatched"] == 0 and rep["errors"] == 0, rep
+        assert rep["completed"] > 0
