@@ -67,7 +67,7 @@ BATCH_SHA256 = "cb594241cefc45d1"
 # ncu counters of one engine_kernel launch per leg, per algorithmic byte of the
 # same launch (ncu --metrics dram__bytes_read.sum, dram__bytes_write.sum,
 # l1tex__m_xbar2l1tex_read_bytes.sum, one launch per leg selected by its NVTX
-# range, bytes_alg from ODPX_Batch_bytes_alg; profiles/engine_kernel_ratios.md):
+# range with --nvtx, bytes_alg from ODPX_Batch_bytes_alg):
 # "batch" is the 512-graph batch with the saved autotuned schedule, C2, C3 and
 # G the configuration graphs with the default schedule.  A launch's L2 read
 # bytes and DRAM traffic are taken as its algorithmic bytes times these ratios.
