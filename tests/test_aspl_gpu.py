@@ -499,3 +499,56 @@ def test_staged_and_direct_adjacency_give_the_same_results(monkeypatch):
         o = oracle.aspl(sp.adjacency, nodes=sp.nodes, symmetries=sp.symmetries, grid=sp.grid, width=sp.width,
                         height=sp.height)
         assert same(r, o)
+
+
+def _ref_shape(c, seed=0):
+    if c["kind"] == "grid":
+        return dict(grid=True, width=c["width"], height=c["height"], degree=c["degree"], length=c.get("length", 0),
+                    symmetries=c["symmetries"], seed=seed)
+    return dict(grid=False, nodes=c["nodes"], degree=c["degree"], symmetries=c["symmetries"], seed=seed)
+
+
+def test_reference_cuda_library_agrees(golden):
+    """The reference's own libodp_cuda.a, rebuilt for sm_103a and run on this
+    GPU in its own process, gives the same diameter, sum and ASPL bits as
+    this library on the golden edge cases and the seeded generator graphs
+    (cases with num_degrees excepted: the timing driver takes none)."""
+    import baseline
+    if not baseline.gpu_available():
+        pytest.skip("the reference CUDA library is not built here")
+    groups = {None: ([], []), "MATRIX_SAVING": ([], [])}
+    for c in golden["cases"]:
+        if c["num_degrees"] is not None:
+            continue
+        env = "MATRIX_SAVING" if c["name"].endswith("_matrix_saving") else None
+        groups[env][0].append(_ref_shape(c))
+        groups[env][1].append(case_adjacency(c))
+    for g in golden["generators"]:
+        if g.get("big"):
+            continue
+        groups[None][0].append(_ref_shape(g, g["seed"]))
+        groups[None][1].append(gen_record_adjacency(og, g, gen_record_edges(og, g)))
+    checked = 0
+    for env, (shapes, adjs) in groups.items():
+        if not shapes:
+            continue
+        ref = baseline.time_gpu(shapes, adjs, reps=1, env={"ODP_ASPL": env} if env else None)
+        for sh, adj, r in zip(shapes, adjs, ref):
+            mine = gpu_aspl(adj, nodes=sh.get("nodes", 0), symmetries=sh["symmetries"], grid=sh["grid"],
+                            width=sh.get("width", 0), height=sh.get("height", 0))
+            assert same(mine, r[:3]), (sh, mine, r[:3])
+            checked += 1
+    assert checked >= 40
+
+
+def test_largest_degree_the_engine_takes():
+    """Degree 508: rows of 508 neighbours (512 with padding), so a staged
+    block holds only 8 rows; results equal the oracle's."""
+    n, d = 1024, 508
+    adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=77), d)
+    want = oracle.aspl(adj, nodes=n)
+    assert same(gpu_aspl(adj, nodes=n), want)
+    b = og.Batch([og.GraphSpec(adj, nodes=n)])
+    assert b.kernel() == "engine"
+    assert same(b.run()[0], want)
+    b.close()
