@@ -368,6 +368,7 @@ def time_configs(args, l2_gbs, hbm_gbs, l2_bytes, nvtx):
         balg = b.bytes_alg()
         info = b.info(0)
         kernel = b.kernel()
+        shape = b.small_shape() if kernel == "small" else None
         nvtx.run(name, lambda: b.time(1, mode=1, flush_mb=args.flush_mb))
         b.close()
         # ODP_Set_aspl end to end: host adjacency, copies and decode included
@@ -392,6 +393,9 @@ def time_configs(args, l2_gbs, hbm_gbs, l2_bytes, nvtx):
                "schedule": {"chunk_words": 1 << info["wc_log2"], "jobs": info["njobs"], "slots": info["nslots"],
                             "tile_rows": info["tile_rows"]},
                "result": {"diameter": r[0], "sum": r[1], "ASPL": r[2]}}
+        if shape:
+            rec["schedule"] = {"chunk_words": 1 << info["wc_log2"], "jobs": info["njobs"], "cluster_ctas": shape[0],
+                               "threads_per_cta": shape[1]}
         ratio = NCU_RATIOS.get(name)
         if ratio:
             # the bound is whichever of L2 reads and DRAM traffic is nearer its ceiling

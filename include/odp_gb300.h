@@ -72,10 +72,16 @@ int  ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots
 /* Which kernel evaluates the plan: 1 when every graph has at most
  * ODP_GB300_SMALL_N (default 2048) vertices, one level of each fits in one
  * CTA's shared memory and the plan has at most one job per SM, so each job
- * runs alone in the small-graph kernel;
+ * runs in the small-graph kernel, on the CTAs of one thread-block cluster;
  * 0 for the persistent engine (mixed plans, explicit schedule settings,
  * change tracking).  Results are the same either way. */
 int  ODPX_Batch_kernel(const ODPX_Batch *batch);
+/* For a plan on the small-graph kernel: the CTAs of the thread-block cluster
+ * that runs each job (1, 2, 4 or 8; each CTA computes its share of the
+ * rows) and the threads per CTA.  Returns 0, or ODPX_ERR_INVALID for a plan
+ * on the persistent engine.  ODP_GB300_SMALL_CLUSTER forces the cluster size
+ * of plans created afterwards (halved until the shape fits). */
+int  ODPX_Batch_small_shape(const ODPX_Batch *batch, int *cluster, int *threads);
 /* Level at which each job (graph x column chunk, plan order) of the last run
  * finished (negative: stalled, i.e. unreachable pairs).  Returns the job count. */
 int  ODPX_Batch_job_levels(const ODPX_Batch *batch, int *levels, int max_jobs);

@@ -40,7 +40,11 @@
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
+#include <string.h>
 #include "odp_engine.h"
+#include <cooperative_groups.h>
+
+namespace cg = cooperative_groups;
 
 #define ENGINE_THREADS 256
 #define ENGINE_WARPS (ENGINE_THREADS / 32)
@@ -743,9 +747,9 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
 /* outcome to pinned host memory, so a call is this one launch.             */
 /* ---------------------------------------------------------------------- */
 
-#define SMALL_THREADS 512
-#define SMALL_WARPS (SMALL_THREADS / 32)
+#define SMALL_THREADS 512        /* most threads per CTA (launches use fewer when the rows are few) */
 #define SMALL_LOADS 8            /* host loads in flight per thread while the table is built */
+#define SMALL_CLUSTER_MAX GBX_SMALL_CLUSTER_MAX   /* CTAs sharing one job (portable cluster size) */
 
 struct SmallOutcome {
   long long sum;
@@ -753,35 +757,55 @@ struct SmallOutcome {
   int stalled;
 };
 
-/* One job (chunk of sources) of a graph whose level fits in shared memory.
- * The same recurrence and bookkeeping as the engine: level 1 from the
- * neighbour lists, then P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]], the
- * bits set per level counted, the job complete when all n * nsrc bits are
- * set and stalled when a level adds none (or the level reaches n).  Thread 0
- * returns the job's share of the sum and its last level. */
+/* Per-CTA bookkeeping of the small kernel (static shared memory). */
+struct SmallShared {
+  gbx_expand_desc desc;
+  unsigned long long total[3];                       /* bits of level k in total[k % 3], from every CTA */
+  unsigned bad[SMALL_CLUSTER_MAX];                   /* rank 0: every CTA's error flag */
+};
+
+/* One job (chunk of sources) of a graph whose level fits in shared memory,
+ * run by the C CTAs of one thread-block cluster.  Every CTA holds both
+ * bitset buffers whole; CTA q computes rows [r0, r1) of each level from its
+ * own copy of the previous level and stores them into the new level's
+ * buffer of every CTA of the cluster (distributed shared memory).  The same
+ * recurrence and bookkeeping as the engine: level 1 from the neighbour
+ * lists, then P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]], the bits set
+ * per level counted, the job complete when all n * nsrc bits are set and
+ * stalled when a level adds none (or the level reaches n).  Each warp adds
+ * its count of a level into the level's total in every CTA (remote atomics)
+ * and one cluster barrier per level orders the rows and the counts; each CTA
+ * then reads the same total and takes the same decision.  The totals rotate
+ * over three slots: the slot of level k + 1 is cleared during level k, after
+ * the barrier that ended every read of it (level k - 2) and before the
+ * barrier after which level k + 1 adds into it.  A CTA writes into another's
+ * shared memory only between two barriers that both pass, so none exits
+ * while another may still write to it.  Thread 0 of each CTA returns the
+ * job's outcome. */
 template <int WC, bool SP>
-__device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b1, SmallOutcome &out)
+__device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b1, int r0, int r1,
+                          SmallShared &sh, SmallOutcome &out)
 {
   typedef RowShape<WC> S;
   constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;
-  __shared__ unsigned long long s_cnt[2];
-  __shared__ int s_go;
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
   const int n = jb.n, dp = jb.dp, d = jb.d, nsrc = jb.nsrc, src0 = jb.src0;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
-  if(threadIdx.x == 0) s_cnt[0] = s_cnt[1] = 0;
-  __syncthreads();
+  const int nrows = r1 - r0;
 
   const unsigned long long full = (unsigned long long)n * (unsigned long long)nsrc;
-  unsigned long long prev = (unsigned long long)nsrc;                 /* thread 0's */
-  long long sum = ((long long)n * nsrc - nsrc) * jb.sym;               /* thread 0's */
+  unsigned long long prev = (unsigned long long)nsrc;
+  long long sum = ((long long)n * nsrc - nsrc) * jb.sym;
   for(int level = 1;; level++){
     const uint4 *X = (level & 1) ? b0 : b1;
     uint4 *Y = (level & 1) ? b1 : b0;
     unsigned cnt = 0;
-    for(int r = warp * S::RPW + sub; r < n; r += SMALL_WARPS * S::RPW){
+    for(int lr = warp * S::RPW + sub; lr < nrows; lr += nwarps * S::RPW){
+      const int r = r0 + lr;
       uint4 a[S::V];
-      const int *ip = idx + r * dp;
+      const int *ip = idx + lr * dp;
       if(level == 1){
 #pragma unroll
         for(int k = 0; k < S::V; k++) a[k] = make_uint4(0u, 0u, 0u, 0u);
@@ -806,106 +830,121 @@ __device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b
             for(int k = 0; k < S::V; k++) or_into(a[k], t[i][k]);
         }
       }
+      uint4 *yr = Y + (size_t)r * S::VPR + gl;
 #pragma unroll
       for(int k = 0; k < S::V; k++){
-        Y[(size_t)r * S::VPR + gl + k * S::G] = a[k];
+        for(int q = 0; q < C; q++) *cl.map_shared_rank(yr + k * S::G, (unsigned)q) = a[k];
         cnt += popc4(a[k]);
       }
     }
     cnt = __reduce_add_sync(0xffffffffu, cnt);
-    if(lane == 0) atomicAdd(&s_cnt[level & 1], (unsigned long long)cnt);
-    __syncthreads();
-    if(threadIdx.x == 0){
-      const unsigned long long c = s_cnt[level & 1];
-      s_cnt[(level + 1) & 1] = 0;
-      const bool complete = c == full;
-      const bool stalled = !complete && (c == prev || level >= n);
-      int go = 0;
-      if(!complete && !stalled){
-        sum += (long long)(full - c) * jb.sym;
-        prev = c;
-        go = 1;
-      }
-      else{
-        out.sum = sum;
-        out.level = level;
-        out.stalled = stalled;
-      }
-      s_go = go;
+    unsigned long long *tot = &sh.total[level % 3];
+    if(lane == 0 && cnt)
+      for(int q = 0; q < C; q++) atomicAdd(cl.map_shared_rank(tot, (unsigned)q), (unsigned long long)cnt);
+    if(threadIdx.x == 0) sh.total[(level + 1) % 3] = 0;
+    cl.sync();
+    const unsigned long long c = *tot;
+    const bool complete = c == full;
+    const bool stalled = !complete && (c == prev || level >= n);
+    if(complete || stalled){
+      out.sum = sum;
+      out.level = level;
+      out.stalled = stalled;
+      break;
     }
-    __syncthreads();
-    if(!s_go) break;
+    sum += (long long)(full - c) * jb.sym;
+    prev = c;
   }
 }
 
-/* One CTA per job.  The job's graph descriptor and the caller's compact
- * adjacency are read from host memory (pinned, or pageable where the device
- * reads it through the host page tables); the row table is built straight
- * into shared memory with the expansion rules of expand_kernel, eight
- * independent host loads in flight per thread.  The job's record (level,
- * error bits, sum, timestamps) goes to pinned host memory. */
+/* One cluster of C CTAs per job (blockIdx.x / C).  The job's graph
+ * descriptor and the caller's compact adjacency are read from host memory
+ * (pinned, or pageable where the device reads it through the host page
+ * tables); each CTA reads 1/C of the adjacency, eight independent host loads
+ * in flight per thread, expands it with the rules of expand_kernel and
+ * stores each entry into the row table of the CTA that owns the row (rows
+ * are split into C equal ranges).  Rank 0 writes the job's record (level,
+ * error bits, sum, timestamps) to pinned host memory.  With `descs` NULL
+ * every job belongs to one graph, whose descriptor is the parameter `desc0`
+ * (a single-graph call then reads no descriptor from host memory). */
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
-small_kernel(const gbx_job *__restrict__ jobs, const gbx_expand_desc *descs, gbx_small_rec *rec)
+small_kernel(const gbx_job *__restrict__ jobs, const gbx_expand_desc *descs, gbx_small_rec *rec,
+             const gbx_expand_desc desc0)
 {
   extern __shared__ __align__(16) unsigned char small_smem[];
-  __shared__ unsigned s_bad;
-  __shared__ gbx_expand_desc s_desc;
-  const int job = blockIdx.x;
+  __shared__ SmallShared sh;
+  cg::cluster_group cl = cg::this_cluster();
+  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int job = blockIdx.x / C;
   const gbx_job jb = jobs[job];
   unsigned long long t_loaded = 0;
   if(threadIdx.x == 0){
     t_loaded = globaltimer();
-    s_desc = descs[jb.graph];
-    s_bad = 0;
+    sh.desc = descs ? descs[jb.graph] : desc0;
+    sh.total[0] = sh.total[1] = sh.total[2] = 0;
   }
-  __syncthreads();
-  const gbx_expand_desc &e = s_desc;
+  /* every CTA of the cluster is running (its shared memory may be written)
+   * and the descriptor is visible to the whole CTA */
+  cl.sync();
+  const gbx_expand_desc &e = sh.desc;
   const int n = jb.n, dp = jb.dp;
+  const int R = (n + C - 1) / C;
+  const int r0 = min(n, rank * R), r1 = min(n, r0 + R);
   const size_t vecs = (size_t)n << (jb.wc_log2 - 1);              /* uint4 per bitset buffer */
   uint4 *b0 = reinterpret_cast<uint4 *>(small_smem);
   uint4 *b1 = b0 + vecs;
-  int *idx = reinterpret_cast<int *>(b1 + vecs);
+  int *idx = reinterpret_cast<int *>(b1 + vecs);                   /* rows [r0, r1) */
 
   bool bad = false;
   const int total = n * dp;
-  for(int t0 = threadIdx.x; t0 < total; t0 += SMALL_THREADS * SMALL_LOADS){
+  const int per = (total + C - 1) / C;
+  const int e0 = min(total, rank * per), e1 = min(total, e0 + per);
+  for(int t0 = e0 + (int)threadIdx.x; t0 < e1; t0 += (int)blockDim.x * SMALL_LOADS){
     int val[SMALL_LOADS], back[SMALL_LOADS];
 #pragma unroll
     for(int k = 0; k < SMALL_LOADS; k++){
-      const int t = t0 + k * SMALL_THREADS;
+      const int t = t0 + k * (int)blockDim.x;
       const int v = t / dp, j = t - v * dp;
       back[k] = 0;
-      val[k] = (t < total && j < e.d) ? e.adj[entry_source(e, v, j, back[k])] : 0;
+      val[k] = (t < e1 && j < e.d) ? e.adj[entry_source(e, v, j, back[k])] : 0;
     }
 #pragma unroll
     for(int k = 0; k < SMALL_LOADS; k++){
-      const int t = t0 + k * SMALL_THREADS;
-      if(t < total){
+      const int t = t0 + k * (int)blockDim.x;
+      if(t < e1){
         const int v = t / dp, j = t - v * dp;
         int deg = e.ndeg ? e.ndeg[v] : e.d;
         if(deg < 0 || deg > e.d){ bad = true; deg = deg < 0 ? 0 : e.d; }
         const int row = e.grid_s ? e.itable[v] : v;
-        idx[row * dp + j] = expand_value(e, val[k], back[k], j, deg, row, bad);
+        const int value = expand_value(e, val[k], back[k], j, deg, row, bad);
+        if((unsigned)row < (unsigned)n){
+          const int owner = row / R;
+          *cl.map_shared_rank(idx + (row - owner * R) * dp + j, (unsigned)owner) = value;
+        }
+        else bad = true;
       }
     }
   }
-  if(bad) atomicOr(&s_bad, 1u);
-  __syncthreads();
+  const unsigned bad_cta = __syncthreads_or(bad);
+  if(threadIdx.x == 0) *cl.map_shared_rank(&sh.bad[rank], 0u) = bad_cta;
+  cl.sync();                                   /* every row table complete */
 
   SmallOutcome o = {0, 0, 0};
 #define ODP_SMALL_CASE(L) case L: \
-    if(jb.srcpos) small_job<(1 << L), true>(jb, idx, b0, b1, o); \
-    else small_job<(1 << L), false>(jb, idx, b0, b1, o); \
+    if(jb.srcpos) small_job<(1 << L), true>(jb, idx, b0, b1, r0, r1, sh, o); \
+    else small_job<(1 << L), false>(jb, idx, b0, b1, r0, r1, sh, o); \
     break;
   switch(jb.wc_log2){
     ODP_SMALL_CASE(1) ODP_SMALL_CASE(2) ODP_SMALL_CASE(3) ODP_SMALL_CASE(4)
     default: break;
   }
 #undef ODP_SMALL_CASE
-  if(threadIdx.x == 0){
+  if(rank == 0 && threadIdx.x == 0){
+    unsigned b = 0;
+    for(int q = 0; q < C; q++) b |= sh.bad[q];
     gbx_small_rec r;
     r.level = o.stalled ? -o.level : o.level;
-    r.err = s_bad ? GBX_ERR_BAD_ADJ : 0u;
+    r.err = b ? GBX_ERR_BAD_ADJ : 0u;
     r.sum = o.sum;
     r.t_loaded = t_loaded;
     r.t_done = globaltimer();
@@ -1067,13 +1106,49 @@ int gbx_small_prepare(void)
   return 0;
 }
 
-int gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, gbx_small_rec *rec,
-                     size_t smem_bytes, void *stream)
+static cudaLaunchConfig_t small_config(int njobs, int cluster, int threads, size_t smem_bytes, cudaStream_t stream,
+                                       cudaLaunchAttribute *attr)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(njobs * cluster), 1, 1);
+  cfg.blockDim = dim3((unsigned)threads, 1, 1);
+  cfg.dynamicSmemBytes = smem_bytes;
+  cfg.stream = stream;
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)cluster;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cfg;
+}
+
+static int small_shape_ok(int cluster, int threads, size_t smem_bytes)
+{
+  return cluster >= 1 && cluster <= SMALL_CLUSTER_MAX && (cluster & (cluster - 1)) == 0 && threads >= 32 &&
+         threads <= SMALL_THREADS && threads % 32 == 0 && smem_bytes <= GBX_SMALL_SMEM_MAX;
+}
+
+int gbx_small_clusters(int cluster, int threads, size_t smem_bytes, int *active)
+{
+  *active = 0;
+  if(!small_shape_ok(cluster, threads, smem_bytes)) return (int)cudaErrorInvalidValue;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = small_config(1, cluster, threads, smem_bytes, 0, attr);
+  return (int)cudaOccupancyMaxActiveClusters(active, small_kernel, &cfg);
+}
+
+int gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, const gbx_expand_desc *desc0,
+                     gbx_small_rec *rec, size_t smem_bytes, int cluster, int threads, void *stream)
 {
   if(njobs <= 0) return 0;
-  if(smem_bytes > GBX_SMALL_SMEM_MAX) return (int)cudaErrorInvalidValue;
-  small_kernel<<<njobs, SMALL_THREADS, smem_bytes, (cudaStream_t)stream>>>(d_jobs, descs, rec);
-  return (int)cudaGetLastError();
+  if(!small_shape_ok(cluster, threads, smem_bytes) || (!descs && !desc0)) return (int)cudaErrorInvalidValue;
+  cudaLaunchAttribute attr[1];
+  cudaLaunchConfig_t cfg = small_config(njobs, cluster, threads, smem_bytes, (cudaStream_t)stream, attr);
+  gbx_expand_desc d0;
+  if(desc0) d0 = *desc0;
+  else memset(&d0, 0, sizeof(d0));
+  return (int)cudaLaunchKernelEx(&cfg, small_kernel, d_jobs, descs, rec, d0);
 }
 
 int gbx_host_device_ptr(void *host, void **dev)

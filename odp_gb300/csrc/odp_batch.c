@@ -100,6 +100,14 @@ int ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots,
 
 int ODPX_Batch_kernel(const ODPX_Batch *batch) { return batch ? batch->small : ODPX_ERR_INVALID; }
 
+int ODPX_Batch_small_shape(const ODPX_Batch *batch, int *cluster, int *threads)
+{
+  if(!batch || !batch->small) return ODPX_ERR_INVALID;
+  if(cluster) *cluster = batch->small_cluster;
+  if(threads) *threads = batch->small_threads;
+  return 0;
+}
+
 /* ODP_Set_aspl_batch keeps the last plan and reuses it (and its CUDA graph)
  * while the shapes and degree tables stay the same. */
 static struct {

@@ -55,6 +55,7 @@ typedef struct {
 /* Shared memory a job of the small-graph kernel may use: its two bitset
  * buffers (2 x n x wc x 8 bytes) and its neighbour table (n x dp x 4). */
 #define GBX_SMALL_SMEM_MAX (200 * 1024)
+#define GBX_SMALL_CLUSTER_MAX 8   /* CTAs (one thread-block cluster) per small-kernel job */
 
 /* Per-slot mutable state, two 128-byte lines each.  The slot holds a copy
  * of its job's descriptor, so a CTA that takes a tile reads everything it
@@ -156,14 +157,21 @@ typedef struct {
   unsigned long long t_loaded, t_done;
 } gbx_small_rec;
 
-/* Jobs [0, njobs) of d_jobs, one CTA each, every level in shared memory
- * (smem_bytes per CTA, at most GBX_SMALL_SMEM_MAX).  Each CTA reads its
- * graph's descriptor descs[job.graph] and the compact adjacency it names
- * (`adj`) from host memory and builds the row table in shared memory; the
- * job's record goes to rec[job].  `descs` and `rec` are device addresses of
- * pinned host memory (gbx_host_device_ptr). */
-int  gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, gbx_small_rec *rec,
-                      size_t smem_bytes, void *stream);
+/* Jobs [0, njobs) of d_jobs, one thread-block cluster of `cluster` CTAs
+ * (1, 2, 4 or 8) of `threads` threads each per job, every level in shared
+ * memory (smem_bytes per CTA, at most GBX_SMALL_SMEM_MAX: both bitset
+ * buffers of the job and the row table of the CTA's 1/cluster of the rows).
+ * The CTAs read their graph's descriptor descs[job.graph] and the compact
+ * adjacency it names (`adj`) from host memory and build the row tables in
+ * shared memory; the job's record goes to rec[job].  `descs` and `rec` are
+ * device addresses of pinned host memory (gbx_host_device_ptr).  With
+ * `descs` NULL every job belongs to graph 0, whose descriptor `*desc0` is
+ * passed by value in the launch's parameters (no host-memory read for it). */
+int  gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, const gbx_expand_desc *desc0,
+                      gbx_small_rec *rec, size_t smem_bytes, int cluster, int threads, void *stream);
+/* How many clusters of that shape the GPU holds at once (0: the shape does
+ * not fit; then it cannot be launched). */
+int  gbx_small_clusters(int cluster, int threads, size_t smem_bytes, int *active);
 /* Device address of pinned host memory. */
 int  gbx_host_device_ptr(void *host, void **dev);
 /* Allows the small-graph kernel GBX_SMALL_SMEM_MAX bytes of shared memory

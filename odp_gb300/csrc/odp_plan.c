@@ -56,6 +56,7 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->reorder = env_int("ODP_GB300_REORDER", 1);
   t->direct = env_int("ODP_GB300_DIRECT", 1);
   t->small_n = env_int("ODP_GB300_SMALL_N", 2048);
+  t->small_cluster = env_int("ODP_GB300_SMALL_CLUSTER", 0);
 }
 
 /* Chunk width (log2 words) for a graph whose whole level runs in one CTA's
@@ -70,9 +71,24 @@ static int small_wc_log2(int n, int dp, int full_l2)
   return 0;
 }
 
-static size_t small_bytes(int n, int dp, int wl)
+/* Shared memory per CTA of the small kernel when `cluster` CTAs share a job:
+ * both bitset buffers whole, the row table of 1/cluster of the rows. */
+static size_t small_bytes(int n, int dp, int wl, int cluster)
 {
-  return 2 * (size_t)n * ((size_t)8 << wl) + (size_t)n * dp * 4;
+  const size_t rows = (size_t)(n + cluster - 1) / (size_t)cluster;
+  return 2 * (size_t)n * ((size_t)8 << wl) + rows * (size_t)dp * 4;
+}
+
+/* Threads per CTA for a CTA's rows: one lane per 16 bytes of a row (at most
+ * a warp per row), rounded up to whole warps, 64 to 512. */
+static int small_threads_for(int n, int wl, int cluster)
+{
+  const int rows = (n + cluster - 1) / cluster;
+  const int lanes = (1 << wl) / 2 < 32 ? (1 << wl) / 2 : 32;
+  long long t = ((long long)rows * lanes + 31) / 32 * 32;
+  if(t < 64) t = 64;
+  if(t > 512) t = 512;
+  return (int)t;
 }
 
 static int ilog2_ceil(long long x)
@@ -338,6 +354,39 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     }
   }
 
+  /* Cluster size: a job's rows are split over the CTAs of one thread-block
+   * cluster, so a plan with few jobs uses more SMs (the n = 1024, d = 8
+   * graph: 8 jobs of 2 words on clusters of 8 CTAs, 64 SMs).  The largest
+   * power of two up to 8 that keeps every CTA on its own SM, among shapes
+   * the GPU can hold; ODP_GB300_SMALL_CLUSTER forces a size (it is halved
+   * until the shape fits). */
+  if(small && gbx_small_prepare()) small = 0;
+  if(small){
+    const int want = tuning->small_cluster;
+    int chosen = 0;
+    for(int c = want > 0 && want <= GBX_SMALL_CLUSTER_MAX ? want : GBX_SMALL_CLUSTER_MAX; c >= 1 && !chosen; c >>= 1){
+      if(want <= 0 && small_jobs * c > sms && c > 1) continue;
+      size_t smem = 0;
+      int threads = 64;
+      for(int i = 0; i < count; i++){
+        const int n = shapes[i].grid ? shapes[i].width * shapes[i].height : shapes[i].nodes;
+        const int dp = ALIGN_UP(shapes[i].degree > 0 ? shapes[i].degree : 1, 4);
+        size_t b = small_bytes(n, dp, small_wl[i], c);
+        int t = small_threads_for(n, small_wl[i], c);
+        if(b > smem) smem = b;
+        if(t > threads) threads = t;
+      }
+      int active = 0;
+      if(smem <= GBX_SMALL_SMEM_MAX && gbx_small_clusters(c, threads, smem, &active) == 0 && active > 0){
+        chosen = c;
+        p->small_cluster = c;
+        p->small_threads = threads;
+        p->small_smem = smem;
+      }
+    }
+    if(!chosen) small = 0;
+  }
+
   /* Shapes, chunk widths, tiles. */
   int njobs = 0;
   for(int i = 0; i < count; i++){
@@ -372,11 +421,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     if(wl < 1) wl = 1;
     if(wl > 7) wl = 7;                 /* rows of at most 1 KB per chunk */
     if(wl > full_l2 && full_l2 >= 1) wl = full_l2;
-    if(small){
-      wl = small_wl[i];
-      size_t b = small_bytes(g->n, g->dp, wl);
-      if(b > p->small_smem) p->small_smem = b;
-    }
+    if(small) wl = small_wl[i];
     g->wc_log2 = wl;
     const int wc = 1 << wl;
     g->nchunks = (g->W + wc - 1) / wc;
@@ -395,7 +440,6 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   p->njobs = njobs;
   p->small = small;
   free(small_wl);
-  if(small && gbx_small_prepare()){ odp_plan_destroy(p); return ODPX_ERR_CUDA; }
 
   /* Tiles: about 640 KB of traffic each, measured best on GB300 for large
    * single graphs and for most size buckets of the batch.  A plan with few
@@ -641,8 +685,13 @@ static int enqueue(odp_plan *p)
 
 int odp_plan_enqueue_engine(odp_plan *p)
 {
-  if(p->small)
-    return gbx_small_launch(p->d_jobs, p->njobs, p->d_small_desc, p->d_small_rec, p->small_smem, p->stream);
+  if(p->small){
+    /* one graph: its descriptor (this call's adjacency pointer) travels in
+     * the launch's parameters, so the plan is launched directly each call */
+    const int one = p->ngraphs == 1;
+    return gbx_small_launch(p->d_jobs, p->njobs, one ? NULL : p->d_small_desc, one ? &p->h_expand[0] : NULL,
+                            p->d_small_rec, p->small_smem, p->small_cluster, p->small_threads, p->stream);
+  }
   return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
                            (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),
                            (gbx_job_out *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->any_active,
@@ -718,7 +767,8 @@ void odp_plan_stage(odp_plan *p, const int *const *adjacency)
 
 int odp_plan_launch(odp_plan *p)
 {
-  if(p->tuning.use_graph){
+  /* a single-graph small plan passes this call's descriptor by value: never captured */
+  if(p->tuning.use_graph && !(p->small && p->ngraphs == 1)){
     if(!p->graph_exec){
       if(gbx_capture_begin(p->stream)) return ODPX_ERR_CUDA;
       int e = enqueue(p);

@@ -33,6 +33,7 @@ typedef struct {
   int reorder;                 /* after the first run, order jobs by their measured duration (1, default) */
   int direct;                  /* pull callers' adjacency from host memory when the device can (1, default) */
   int small_n;                 /* graphs of at most this many vertices may run in shared memory (0: never) */
+  int small_cluster;           /* CTAs per small-kernel job: 1, 2, 4 or 8; 0 = automatic */
 } odp_tuning;
 
 typedef struct {
@@ -74,6 +75,8 @@ typedef struct odp_plan {
   gbx_expand_desc *h_expand;   /* pinned copy of the expand descriptors (direct plans) */
   int small;                   /* every job runs in the small-graph kernel, in shared memory */
   size_t small_smem;           /* shared memory per CTA of the small-graph kernel */
+  int small_cluster;           /* CTAs (one thread-block cluster) per job of the small-graph kernel */
+  int small_threads;           /* threads per CTA of the small-graph kernel */
   gbx_small_rec *h_small_rec;  /* small plans: per-job records, pinned; the kernel writes them */
   gbx_small_rec *d_small_rec;  /*   the same memory, as the device addresses it */
   gbx_expand_desc *d_small_desc; /* small plans: h_expand as the device addresses it */

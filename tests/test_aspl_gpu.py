@@ -243,6 +243,45 @@ def test_small_graph_kernel_and_engine_agree(small_n, monkeypatch):
     b.close()
 
 
+@pytest.mark.parametrize("cluster", [1, 2, 4, 8])
+def test_small_kernel_cluster_sizes(cluster, monkeypatch):
+    """A small-kernel job runs on the CTAs of one thread-block cluster: each
+    CTA computes its share of the rows and stores them into every CTA's copy
+    of the level (distributed shared memory), and each builds the row-table
+    entries of 1/cluster of the adjacency for the CTAs that own the rows.
+    Forced cluster sizes of 1 to 8 CTAs give the oracle's results on row
+    counts that do not divide evenly (n = 998, 1000) or are below the
+    cluster size (n = 5, 6), symmetric general and grid graphs (rows placed
+    through the rotation table), irregular and disconnected graphs, and the
+    n = 1024 golden graph, one plan per graph and as one plan."""
+    monkeypatch.setenv("ODP_GB300_SMALL_CLUSTER", str(cluster))
+    g = lambda n, d, s=1, seed=1: og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, s, seed=seed), d, s)
+    cases = _saturation_cases()
+    cases += [og.GraphSpec(g(n, d, seed=20 + n), nodes=n) for n, d in ((998, 3), (1000, 6), (6, 3), (5, 4), (1024, 8))]
+    for s_, w in ((2, 20), (4, 20)):
+        e = og.generate_random_grid(w, w, 4, 3, s_, seed=13)
+        cases.append(og.GraphSpec(og.conv_edge2adjacency_grid(w, w, e, 4, s_), grid=True, width=w, height=w,
+                                  symmetries=s_))
+    refs = [oracle.aspl(c.adjacency, nodes=c.nodes, num_degrees=c.num_degrees, symmetries=c.symmetries,
+                        grid=c.grid, width=c.width, height=c.height) for c in cases]
+    for k, (c, y) in enumerate(zip(cases, refs)):
+        b = og.Batch([c])
+        assert b.kernel() == "small"
+        assert b.small_shape()[0] == cluster
+        assert same(b.run()[0], y), (k, cluster)
+        assert same(b.run()[0], y), (k, cluster)
+        b.close()
+    b = og.Batch(cases)
+    assert b.kernel() == "small" and b.small_shape()[0] == cluster
+    for k, (x, y) in enumerate(zip(b.run(), refs)):
+        assert same(x, y), (k, cluster)
+    b.close()
+    monkeypatch.delenv("ODP_GB300_SMALL_CLUSTER")
+    b = og.Batch([cases[-3]])                                  # n = 1024, d = 8: 8 jobs on clusters of 8
+    assert b.small_shape()[0] == 8
+    b.close()
+
+
 def test_config1_default_kind_and_saving():
     n, d = 1024, 8
     adj = og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=1), d)
