@@ -70,11 +70,13 @@ unsigned long long ODPX_Batch_tiles(const ODPX_Batch *batch);
 /* Introspection for benchmarks: jobs, slots, chunk width (log2 words) of graph i. */
 int  ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots, int *wc_log2, int *tile_rows);
 /* Which kernel evaluates the plan: 1 when every graph has at most
- * ODP_GB300_SMALL_N (default 2048) vertices, one level of each fits in one
- * CTA's shared memory and the plan has at most one job per SM, so each job
- * runs in the small-graph kernel, on the CTAs of one thread-block cluster;
- * 0 for the persistent engine (mixed plans, explicit schedule settings,
- * change tracking).  Results are the same either way. */
+ * ODP_GB300_SMALL_N (default 8192) vertices, both bitset buffers of a column
+ * chunk of at least 128 sources fit in one CTA's shared memory beside its
+ * share of the row table, and the plan's CTAs fit on the SMs in one wave, so
+ * each job runs in the small-graph kernel, on the CTAs
+ * of one thread-block cluster; 0 for the persistent engine (larger or mixed
+ * plans, explicit schedule settings, change tracking).  Results are the same
+ * either way. */
 int  ODPX_Batch_kernel(const ODPX_Batch *batch);
 /* For a plan on the small-graph kernel: the CTAs of the thread-block cluster
  * that runs each job (1, 2, 4 or 8; each CTA computes its share of the

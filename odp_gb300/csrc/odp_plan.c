@@ -55,17 +55,19 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->local_kb_explicit = getenv("ODP_GB300_LOCAL_KB") != NULL;
   t->reorder = env_int("ODP_GB300_REORDER", 1);
   t->direct = env_int("ODP_GB300_DIRECT", 1);
-  t->small_n = env_int("ODP_GB300_SMALL_N", 2048);
+  t->small_n = env_int("ODP_GB300_SMALL_N", 8192);
   t->small_cluster = env_int("ODP_GB300_SMALL_CLUSTER", 0);
 }
 
-/* Chunk width (log2 words) for a graph whose whole level runs in one CTA's
- * shared memory: the widest of at most 16 words, and at most the graph's own
- * width, whose two bitset buffers and neighbour table fit; 0 if none does. */
-static int small_wc_log2(int n, int dp, int full_l2)
+/* Chunk width (log2 words) for a graph whose whole level runs in shared
+ * memory on a cluster of `cluster` CTAs: the widest of at most 16 words, and
+ * at most the graph's own width, whose two bitset buffers (whole in every
+ * CTA) and row table (1/cluster of the rows per CTA) fit; 0 if none does. */
+static int small_wc_log2(int n, int dp, int full_l2, int cluster)
 {
+  const size_t rows = (size_t)(n + cluster - 1) / (size_t)cluster;
   for(int wl = full_l2 < 4 ? full_l2 : 4; wl >= 1; wl--){
-    size_t bytes = 2 * (size_t)n * ((size_t)8 << wl) + (size_t)n * dp * 4;
+    size_t bytes = 2 * (size_t)n * ((size_t)8 << wl) + rows * (size_t)dp * 4;
     if(bytes <= GBX_SMALL_SMEM_MAX) return wl;
   }
   return 0;
@@ -285,6 +287,88 @@ static int tracks_changes(const odp_tuning *t, int count, int grid, int n, int s
   return t->activity == -1 ? grid : t->activity;
 }
 
+static int shape_n(const odp_shape *sh) { return sh->grid ? sh->width * sh->height : sh->nodes; }
+static int shape_dp(const odp_shape *sh) { return ALIGN_UP(sh->degree > 0 ? sh->degree : 1, 4); }
+static int shape_words(const odp_shape *sh) { return (shape_n(sh) / sh->symmetries + 63) / 64; }
+
+/* Jobs of the small kernel with these chunk widths. */
+static long long small_job_count(const odp_shape *shapes, int count, const int *wl)
+{
+  long long jobs = 0;
+  for(int i = 0; i < count; i++) jobs += (shape_words(&shapes[i]) + (1 << wl[i]) - 1) >> wl[i];
+  return jobs;
+}
+
+/* Whether a plan runs on the small-graph kernel, and its shape: the chunk
+ * width of each graph (wl), the CTAs per job (one thread-block cluster), the
+ * threads and shared memory per CTA.  Every graph must have at most small_n
+ * vertices and no schedule setting or change tracking may ask for the
+ * engine.  The cluster is the largest power of two up to 8 at which every
+ * graph fits and every CTA of the plan gets its own SM; for each graph the
+ * widest chunk that fits is halved, widest first, while the jobs still fit on
+ * the SMs (the n = 1024, d = 8 graph: 8 jobs of 2 words on clusters of 8
+ * CTAs, 64 SMs).  Plans that would need more than one wave of CTAs stay on
+ * the persistent engine: every job reads its graph's adjacency from host
+ * memory, and on GB300 the n = 4096, d = 24 and 32 graphs (32 jobs on
+ * clusters of 8, two waves) took 151 and 257 us in the small kernel against
+ * 84 and 95 us in the engine, while one-wave graphs up to n = 4096 gained
+ * (n = 4096, d = 8: 55 against 85 us; a 64 x 64 grid: 176 against 418 us).
+ * A cluster size forced by ODP_GB300_SMALL_CLUSTER is used if the graphs fit
+ * at it (else halved), whatever the SM count. */
+static int choose_small(const odp_shape *shapes, int count, const odp_tuning *t, int sms, int *wl,
+                        int *cluster_out, int *threads_out, size_t *smem_out)
+{
+  if(count <= 0 || t->small_n <= 0 || t->wc_log2 > 0 || t->slots > 0 || t->tile_rows > 0 || t->local_kb_explicit)
+    return 0;
+  for(int i = 0; i < count; i++){
+    const int n = shape_n(&shapes[i]);
+    const ODPX_Tune_entry *te = table_lookup(n, shapes[i].degree, shapes[i].grid);
+    if(n > t->small_n || (te && te->wc_log2 > 0) || tracks_changes(t, count, shapes[i].grid, n, shapes[i].symmetries))
+      return 0;
+  }
+  if(gbx_small_prepare()) return 0;
+  const int want = t->small_cluster > 0 && t->small_cluster <= GBX_SMALL_CLUSTER_MAX ? t->small_cluster : 0;
+  {
+    for(int c = want ? want : GBX_SMALL_CLUSTER_MAX; c >= 1; c >>= 1){
+      int ok = 1;
+      for(int i = 0; i < count && ok; i++){
+        const int W = shape_words(&shapes[i]);
+        wl[i] = small_wc_log2(shape_n(&shapes[i]), shape_dp(&shapes[i]), ilog2_ceil(W < 2 ? 2 : W), c);
+        if(!wl[i]) ok = 0;
+      }
+      if(!ok) continue;
+      long long jobs = small_job_count(shapes, count, wl);
+      if(!want && jobs * c > sms) continue;
+      for(;;){                                   /* narrower chunks while the jobs fit on the SMs */
+        int k = -1;
+        for(int i = 0; i < count; i++)
+          if(wl[i] > 1 && (k < 0 || wl[i] > wl[k])) k = i;
+        if(k < 0) break;
+        wl[k]--;
+        const long long more = small_job_count(shapes, count, wl);
+        if(more * c > sms){ wl[k]++; break; }
+        jobs = more;
+      }
+      size_t smem = 0;
+      int threads = 64;
+      for(int i = 0; i < count; i++){
+        const size_t b = small_bytes(shape_n(&shapes[i]), shape_dp(&shapes[i]), wl[i], c);
+        const int th = small_threads_for(shape_n(&shapes[i]), wl[i], c);
+        if(b > smem) smem = b;
+        if(th > threads) threads = th;
+      }
+      int active = 0;
+      if(smem <= GBX_SMALL_SMEM_MAX && gbx_small_clusters(c, threads, smem, &active) == 0 && active > 0){
+        *cluster_out = c;
+        *threads_out = threads;
+        *smem_out = smem;
+        return 1;
+      }
+    }
+  }
+  return 0;
+}
+
 #define CK(call) do{ int _e = (call); if(_e){ rc = ODPX_ERR_CUDA; goto fail; } }while(0)
 
 int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning, odp_plan **out)
@@ -307,85 +391,14 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   const double budget = (double)tuning->l2_budget_mb * 1024.0 * 1024.0;
   const double local_bytes = (double)tuning->local_kb * 1024.0;
 
-  /* A small plan: every graph has at most small_n vertices and one level of
-   * it (both bitset buffers and the neighbour table) fits in one CTA's shared
-   * memory, so each job runs alone in the small-graph kernel, with no
+  /* A small plan: every job runs in the small-graph kernel, its bitsets and
+   * row table in the shared memory of one thread-block cluster, with no
    * device-wide hand-off per level.  Mixed plans keep every job in the
-   * persistent engine, whose short jobs fill the end of a run.  Explicit
-   * schedule settings (chunk width, slots, tile rows, one-CTA threshold, a
-   * chunk width from the tuning table) and change tracking select the engine. */
-  int small = count > 0 && tuning->small_n > 0 && tuning->wc_log2 == 0 && tuning->slots == 0 &&
-              tuning->tile_rows == 0 && !tuning->local_kb_explicit;
-  int *small_wl = calloc((size_t)count, sizeof(int));
-  long long small_jobs = 0;
-  for(int i = 0; i < count && small; i++){
-    const odp_shape *sh = &shapes[i];
-    const int n = sh->grid ? sh->width * sh->height : sh->nodes;
-    const int dp = ALIGN_UP(sh->degree > 0 ? sh->degree : 1, 4);
-    const int W = (n / sh->symmetries + 63) / 64;
-    const ODPX_Tune_entry *te = table_lookup(n, sh->degree, sh->grid);
-    small_wl[i] = small_wc_log2(n, dp, ilog2_ceil(W < 2 ? 2 : W));
-    if(n > tuning->small_n || (te && te->wc_log2 > 0) || tracks_changes(tuning, count, sh->grid, n, sh->symmetries) ||
-       !small_wl[i])
-      small = 0;
-    small_jobs += (W + (1 << small_wl[i]) - 1) >> small_wl[i];
-  }
-  /* Each job takes one SM.  A plan with more jobs than SMs stays on the
-   * engine, which keeps four CTAs per SM busy with them (the small kernel is
-   * measured on single graphs and small groups only).  Narrower chunks give a
-   * plan with few jobs more of them (the n = 1024, d = 8 graph: 2 jobs of 8
-   * words, or 8 of 2 words, each gathering a quarter of the bytes), until the
-   * jobs cover the SMs. */
+   * persistent engine, whose short jobs fill the end of a run. */
   const int sms = g_sm_count > 0 ? g_sm_count : 1;
-  if(small && small_jobs > sms) small = 0;
-  if(small){
-    while(small_jobs < sms){
-      int k = -1;
-      for(int i = 0; i < count; i++)
-        if(small_wl[i] > 1 && (k < 0 || small_wl[i] > small_wl[k])) k = i;
-      if(k < 0) break;
-      const int n = shapes[k].grid ? shapes[k].width * shapes[k].height : shapes[k].nodes;
-      const int W = (n / shapes[k].symmetries + 63) / 64;
-      const long long more = ((W + (1 << (small_wl[k] - 1)) - 1) >> (small_wl[k] - 1)) -
-                             ((W + (1 << small_wl[k]) - 1) >> small_wl[k]);
-      if(small_jobs + more > sms) break;       /* halving this graph's chunks would pass one job per SM */
-      small_jobs += more;
-      small_wl[k]--;
-    }
-  }
-
-  /* Cluster size: a job's rows are split over the CTAs of one thread-block
-   * cluster, so a plan with few jobs uses more SMs (the n = 1024, d = 8
-   * graph: 8 jobs of 2 words on clusters of 8 CTAs, 64 SMs).  The largest
-   * power of two up to 8 that keeps every CTA on its own SM, among shapes
-   * the GPU can hold; ODP_GB300_SMALL_CLUSTER forces a size (it is halved
-   * until the shape fits). */
-  if(small && gbx_small_prepare()) small = 0;
-  if(small){
-    const int want = tuning->small_cluster;
-    int chosen = 0;
-    for(int c = want > 0 && want <= GBX_SMALL_CLUSTER_MAX ? want : GBX_SMALL_CLUSTER_MAX; c >= 1 && !chosen; c >>= 1){
-      if(want <= 0 && small_jobs * c > sms && c > 1) continue;
-      size_t smem = 0;
-      int threads = 64;
-      for(int i = 0; i < count; i++){
-        const int n = shapes[i].grid ? shapes[i].width * shapes[i].height : shapes[i].nodes;
-        const int dp = ALIGN_UP(shapes[i].degree > 0 ? shapes[i].degree : 1, 4);
-        size_t b = small_bytes(n, dp, small_wl[i], c);
-        int t = small_threads_for(n, small_wl[i], c);
-        if(b > smem) smem = b;
-        if(t > threads) threads = t;
-      }
-      int active = 0;
-      if(smem <= GBX_SMALL_SMEM_MAX && gbx_small_clusters(c, threads, smem, &active) == 0 && active > 0){
-        chosen = c;
-        p->small_cluster = c;
-        p->small_threads = threads;
-        p->small_smem = smem;
-      }
-    }
-    if(!chosen) small = 0;
-  }
+  int *small_wl = calloc((size_t)count, sizeof(int));
+  int small = choose_small(shapes, count, tuning, sms, small_wl, &p->small_cluster, &p->small_threads,
+                           &p->small_smem);
 
   /* Shapes, chunk widths, tiles. */
   int njobs = 0;

@@ -237,7 +237,7 @@ def test_small_graph_kernel_and_engine_agree(small_n, monkeypatch):
         assert b.kernel() == kernel
         assert same(b.run()[0], y)
         b.close()
-    big = og.GraphSpec(g(4096, 8, seed=14), nodes=4096)                 # one graph too large mixes in: engine
+    big = og.GraphSpec(g(8192, 8, seed=14), nodes=8192)                 # one graph too large mixes in: engine
     b = og.Batch(cases[:2] + [big])
     assert b.kernel() == "engine"
     b.close()
@@ -280,6 +280,25 @@ def test_small_kernel_cluster_sizes(cluster, monkeypatch):
     b = og.Batch([cases[-3]])                                  # n = 1024, d = 8: 8 jobs on clusters of 8
     assert b.small_shape()[0] == 8
     b.close()
+
+
+def test_small_kernel_mid_size_graphs():
+    """With the row table split over a cluster, graphs up to n = 4096 whose
+    bitset buffers fit run in the small kernel when their jobs fit on the SMs
+    in one wave; a graph that would need two waves runs in the engine.  Both
+    give the oracle's results."""
+    g = lambda n, d, seed: og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=seed), d)
+    e = og.generate_random_grid(64, 64, 6, 3, 1, seed=3)
+    cases = [(og.GraphSpec(g(3000, 16, 31), nodes=3000), "small"),
+             (og.GraphSpec(g(4096, 8, 32), nodes=4096), "small"),
+             (og.GraphSpec(og.conv_edge2adjacency_grid(64, 64, e, 6, 1), grid=True, width=64, height=64), "small"),
+             (og.GraphSpec(g(4096, 24, 33), nodes=4096), "engine")]
+    for c, kernel in cases:
+        want = oracle.aspl(c.adjacency, nodes=c.nodes, grid=c.grid, width=c.width, height=c.height)
+        b = og.Batch([c])
+        assert b.kernel() == kernel, (c.nodes, kernel)
+        assert same(b.run()[0], want)
+        b.close()
 
 
 def test_config1_default_kind_and_saving():
