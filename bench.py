@@ -395,7 +395,7 @@ def time_configs(args, l2_gbs, hbm_gbs, l2_bytes, nvtx):
                "result": {"diameter": r[0], "sum": r[1], "ASPL": r[2]}}
         if shape:
             rec["schedule"] = {"chunk_words": 1 << info["wc_log2"], "jobs": info["njobs"], "cluster_ctas": shape[0],
-                               "threads_per_cta": shape[1]}
+                               "threads_per_cta": shape[1], "rows_partitioned": bool(shape[2])}
         ratio = NCU_RATIOS.get(name)
         if ratio:
             # the bound is whichever of L2 reads and DRAM traffic is nearer its ceiling

@@ -80,10 +80,14 @@ int  ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots
 int  ODPX_Batch_kernel(const ODPX_Batch *batch);
 /* For a plan on the small-graph kernel: the CTAs of the thread-block cluster
  * that runs each job (1, 2, 4 or 8; each CTA computes its share of the
- * rows) and the threads per CTA.  Returns 0, or ODPX_ERR_INVALID for a plan
- * on the persistent engine.  ODP_GB300_SMALL_CLUSTER forces the cluster size
- * of plans created afterwards (halved until the shape fits). */
-int  ODPX_Batch_small_shape(const ODPX_Batch *batch, int *cluster, int *threads);
+ * rows), the threads per CTA, and whether the bitsets are partitioned over
+ * the cluster (1: each CTA holds its own rows and reads the others' from
+ * their shared memory; 0: each CTA holds the whole level).  Returns 0, or
+ * ODPX_ERR_INVALID for a plan on the persistent engine.
+ * ODP_GB300_SMALL_CLUSTER forces the cluster size of plans created
+ * afterwards (halved until the shape fits), ODP_GB300_SMALL_PART=0 or 1 the
+ * layout. */
+int  ODPX_Batch_small_shape(const ODPX_Batch *batch, int *cluster, int *threads, int *partitioned);
 /* Level at which each job (graph x column chunk, plan order) of the last run
  * finished (negative: stalled, i.e. unreachable pairs).  Returns the job count. */
 int  ODPX_Batch_job_levels(const ODPX_Batch *batch, int *levels, int max_jobs);

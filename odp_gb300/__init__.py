@@ -104,7 +104,7 @@ def load():
         "ODPX_Batch_set_wait_limit": (None, [P, ctypes.c_ulonglong]),
         "ODPX_Batch_bytes_alg": (ctypes.c_double, [P]),
         "ODPX_Batch_kernel": (I, [P]),
-        "ODPX_Batch_small_shape": (I, [P, IP, IP]),
+        "ODPX_Batch_small_shape": (I, [P, IP, IP, IP]),
         "ODPX_Measure_l2_read_gbs": (ctypes.c_double, [I, I]),
         "ODPX_Set_tuning": (None, [I, I, I, I, I, I]),
         "ODPX_Current_plan": (P, []),
@@ -496,10 +496,11 @@ class Batch:
         return "small" if load().ODPX_Batch_kernel(self._h) == 1 else "engine"
 
     def small_shape(self):
-        """(cluster CTAs per job, threads per CTA) of a plan on the small-graph kernel."""
-        c, t = ctypes.c_int(), ctypes.c_int()
-        _check(load().ODPX_Batch_small_shape(self._h, ctypes.byref(c), ctypes.byref(t)), "ODPX_Batch_small_shape")
-        return c.value, t.value
+        """(cluster CTAs per job, threads per CTA, partitioned 0/1) of a plan on the small-graph kernel."""
+        c, t, q = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        _check(load().ODPX_Batch_small_shape(self._h, ctypes.byref(c), ctypes.byref(t), ctypes.byref(q)),
+               "ODPX_Batch_small_shape")
+        return c.value, t.value, q.value
 
     def job_levels(self):
         """Per-job finishing level of the last run (plan order; negative: stalled)."""

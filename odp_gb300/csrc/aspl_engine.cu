@@ -764,32 +764,61 @@ struct SmallShared {
   unsigned bad[SMALL_CLUSTER_MAX];                   /* rank 0: every CTA's error flag */
 };
 
+/* Distributed shared memory: the address of a CTA-local shared address in
+ * CTA `rank` of the cluster, and a 16-byte load from such an address. */
+__device__ __forceinline__ unsigned dsmem_map(unsigned local, unsigned rank)
+{
+  unsigned r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(local), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ uint4 dsmem_ld16(unsigned addr)
+{
+  uint4 v;
+  asm volatile("ld.shared::cluster.v4.u32 {%0, %1, %2, %3}, [%4];"
+               : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "r"(addr) : "memory");
+  return v;
+}
+
+/* Row-table entries of the partitioned small kernel: the owning CTA in the
+ * top bits, the row within the owner's range below. */
+#define SMALL_OWNER_SHIFT 24
+#define SMALL_LOCAL_MASK ((1 << SMALL_OWNER_SHIFT) - 1)
+
 /* One job (chunk of sources) of a graph whose level fits in shared memory,
- * run by the C CTAs of one thread-block cluster.  Every CTA holds both
- * bitset buffers whole; CTA q computes rows [r0, r1) of each level from its
- * own copy of the previous level and stores them into the new level's
- * buffer of every CTA of the cluster (distributed shared memory).  The same
- * recurrence and bookkeeping as the engine: level 1 from the neighbour
- * lists, then P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]], the bits set
- * per level counted, the job complete when all n * nsrc bits are set and
- * stalled when a level adds none (or the level reaches n).  Each warp adds
- * its count of a level into the level's total in every CTA (remote atomics)
- * and one cluster barrier per level orders the rows and the counts; each CTA
- * then reads the same total and takes the same decision.  The totals rotate
- * over three slots: the slot of level k + 1 is cleared during level k, after
- * the barrier that ended every read of it (level k - 2) and before the
- * barrier after which level k + 1 adds into it.  A CTA writes into another's
- * shared memory only between two barriers that both pass, so none exits
- * while another may still write to it.  Thread 0 of each CTA returns the
- * job's outcome. */
-template <int WC, bool SP>
-__device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b1, int r0, int r1,
+ * run by the C CTAs of one thread-block cluster; CTA q computes rows
+ * [r0, r1) of each level.  Two layouts:
+ *  - replicated (PART false): every CTA holds both bitset buffers whole,
+ *    gathers from its own copy of the previous level and stores each row it
+ *    computes into the new level's buffer of every CTA of the cluster;
+ *  - partitioned (PART true): every CTA holds only its own rows of both
+ *    buffers and gathers each neighbour row from the CTA that owns it
+ *    (row-table entries name the owner and the row within its range), so a
+ *    graph C times larger fits.  Every gather goes through the cluster's
+ *    shared-memory window, own rows included: on GB300 a separate local path
+ *    (a branch, or a generic address) measured no faster.
+ * The same recurrence and bookkeeping as the engine: level 1 from the
+ * neighbour lists, then P_k[v] = P_{k-1}[v] | OR_j P_{k-1}[nbr[v][j]], the
+ * bits set per level counted, the job complete when all n * nsrc bits are
+ * set and stalled when a level adds none (or the level reaches n).  Each warp
+ * adds its count of a level into the level's total in every CTA (remote
+ * atomics) and one cluster barrier per level orders the rows and the counts;
+ * each CTA then reads the same total and takes the same decision.  The
+ * totals rotate over three slots: the slot of level k + 1 is cleared during
+ * level k, after the barrier that ended every read of it (level k - 2) and
+ * before the barrier after which level k + 1 adds into it.  A CTA reads or
+ * writes another's shared memory only between two barriers that both pass,
+ * so none exits while another may still access it.  Thread 0 of each CTA
+ * returns the job's outcome. */
+template <int WC, bool SP, bool PART>
+__device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b1, int r0, int r1, int R,
                           SmallShared &sh, SmallOutcome &out)
 {
   typedef RowShape<WC> S;
   constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;
   cg::cluster_group cl = cg::this_cluster();
-  const int C = (int)cl.num_blocks(), rank = (int)cl.block_rank();
+  const int C = (int)cl.num_blocks();
   const int n = jb.n, dp = jb.dp, d = jb.d, nsrc = jb.nsrc, src0 = jb.src0;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
@@ -801,28 +830,46 @@ __device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b
   for(int level = 1;; level++){
     const uint4 *X = (level & 1) ? b0 : b1;
     uint4 *Y = (level & 1) ? b1 : b0;
+    const unsigned xs = (unsigned)__cvta_generic_to_shared(X) + 16u * (unsigned)gl;
     unsigned cnt = 0;
     for(int lr = warp * S::RPW + sub; lr < nrows; lr += nwarps * S::RPW){
       const int r = r0 + lr;
+      const int own = PART ? lr : r;                 /* the row's place in this CTA's buffers */
       uint4 a[S::V];
       const int *ip = idx + lr * dp;
       if(level == 1){
 #pragma unroll
         for(int k = 0; k < S::V; k++) a[k] = make_uint4(0u, 0u, 0u, 0u);
         mark_source<WC>(a, source_of<SP>(jb.srcpos, r) - src0, nsrc, gl);
-        for(int j = 0; j < dp; j++) mark_source<WC>(a, source_of<SP>(jb.srcpos, ip[j]) - src0, nsrc, gl);
+        for(int j = 0; j < dp; j++){
+          int u = ip[j];
+          if(PART) u = (u >> SMALL_OWNER_SHIFT) * R + (u & SMALL_LOCAL_MASK);
+          mark_source<WC>(a, source_of<SP>(jb.srcpos, u) - src0, nsrc, gl);
+        }
       }
       else{
 #pragma unroll
-        for(int k = 0; k < S::V; k++) a[k] = X[(size_t)r * S::VPR + gl + k * S::G];
+        for(int k = 0; k < S::V; k++) a[k] = X[(size_t)own * S::VPR + gl + k * S::G];
         for(int j = 0; j < d; j += NB){
           uint4 t[NB][S::V];
 #pragma unroll
           for(int i = 0; i < NB; i++){
             const bool ok = j + i < d;
-            const uint4 *nr = X + (size_t)ip[ok ? j + i : j] * S::VPR + gl;
+            const int u = ip[ok ? j + i : j];
+            if(PART){
+              /* a generic address: this CTA's own shared window for its own
+               * rows, the owner's window in the cluster for the others' */
+              const unsigned base = dsmem_map(xs + 16u * (unsigned)((u & SMALL_LOCAL_MASK) * S::VPR),
+                                              (unsigned)(u >> SMALL_OWNER_SHIFT));
 #pragma unroll
-            for(int k = 0; k < S::V; k++) t[i][k] = ok ? nr[k * S::G] : make_uint4(0u, 0u, 0u, 0u);
+              for(int k = 0; k < S::V; k++)
+                t[i][k] = ok ? dsmem_ld16(base + 16u * (unsigned)(k * S::G)) : make_uint4(0u, 0u, 0u, 0u);
+            }
+            else{
+              const uint4 *nr = X + (size_t)u * S::VPR + gl;
+#pragma unroll
+              for(int k = 0; k < S::V; k++) t[i][k] = ok ? nr[k * S::G] : make_uint4(0u, 0u, 0u, 0u);
+            }
           }
 #pragma unroll
           for(int i = 0; i < NB; i++)
@@ -830,10 +877,12 @@ __device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b
             for(int k = 0; k < S::V; k++) or_into(a[k], t[i][k]);
         }
       }
-      uint4 *yr = Y + (size_t)r * S::VPR + gl;
+      uint4 *yr = Y + (size_t)own * S::VPR + gl;
 #pragma unroll
       for(int k = 0; k < S::V; k++){
-        for(int q = 0; q < C; q++) *cl.map_shared_rank(yr + k * S::G, (unsigned)q) = a[k];
+        if(PART) yr[k * S::G] = a[k];
+        else
+          for(int q = 0; q < C; q++) *cl.map_shared_rank(yr + k * S::G, (unsigned)q) = a[k];
         cnt += popc4(a[k]);
       }
     }
@@ -863,13 +912,15 @@ __device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b
  * tables); each CTA reads 1/C of the adjacency, eight independent host loads
  * in flight per thread, expands it with the rules of expand_kernel and
  * stores each entry into the row table of the CTA that owns the row (rows
- * are split into C equal ranges).  Rank 0 writes the job's record (level,
+ * are split into C equal ranges; with `part` set the entries name the owner
+ * of each neighbour row and the bitset buffers hold only the CTA's own rows).
+ * Rank 0 writes the job's record (level,
  * error bits, sum, timestamps) to pinned host memory.  With `descs` NULL
  * every job belongs to one graph, whose descriptor is the parameter `desc0`
  * (a single-graph call then reads no descriptor from host memory). */
 __global__ void __launch_bounds__(SMALL_THREADS, 1)
 small_kernel(const gbx_job *__restrict__ jobs, const gbx_expand_desc *descs, gbx_small_rec *rec,
-             const gbx_expand_desc desc0)
+             const gbx_expand_desc desc0, const int part)
 {
   extern __shared__ __align__(16) unsigned char small_smem[];
   __shared__ SmallShared sh;
@@ -890,7 +941,7 @@ small_kernel(const gbx_job *__restrict__ jobs, const gbx_expand_desc *descs, gbx
   const int n = jb.n, dp = jb.dp;
   const int R = (n + C - 1) / C;
   const int r0 = min(n, rank * R), r1 = min(n, r0 + R);
-  const size_t vecs = (size_t)n << (jb.wc_log2 - 1);              /* uint4 per bitset buffer */
+  const size_t vecs = (size_t)(part ? R : n) << (jb.wc_log2 - 1);  /* uint4 per bitset buffer */
   uint4 *b0 = reinterpret_cast<uint4 *>(small_smem);
   uint4 *b1 = b0 + vecs;
   int *idx = reinterpret_cast<int *>(b1 + vecs);                   /* rows [r0, r1) */
@@ -916,7 +967,11 @@ small_kernel(const gbx_job *__restrict__ jobs, const gbx_expand_desc *descs, gbx
         int deg = e.ndeg ? e.ndeg[v] : e.d;
         if(deg < 0 || deg > e.d){ bad = true; deg = deg < 0 ? 0 : e.d; }
         const int row = e.grid_s ? e.itable[v] : v;
-        const int value = expand_value(e, val[k], back[k], j, deg, row, bad);
+        int value = expand_value(e, val[k], back[k], j, deg, row, bad);
+        if(part){
+          const int vo = value / R;
+          value = (vo << SMALL_OWNER_SHIFT) | (value - vo * R);
+        }
         if((unsigned)row < (unsigned)n){
           const int owner = row / R;
           *cl.map_shared_rank(idx + (row - owner * R) * dp + j, (unsigned)owner) = value;
@@ -931,8 +986,14 @@ small_kernel(const gbx_job *__restrict__ jobs, const gbx_expand_desc *descs, gbx
 
   SmallOutcome o = {0, 0, 0};
 #define ODP_SMALL_CASE(L) case L: \
-    if(jb.srcpos) small_job<(1 << L), true>(jb, idx, b0, b1, r0, r1, sh, o); \
-    else small_job<(1 << L), false>(jb, idx, b0, b1, r0, r1, sh, o); \
+    if(part){ \
+      if(jb.srcpos) small_job<(1 << L), true, true>(jb, idx, b0, b1, r0, r1, R, sh, o); \
+      else small_job<(1 << L), false, true>(jb, idx, b0, b1, r0, r1, R, sh, o); \
+    } \
+    else{ \
+      if(jb.srcpos) small_job<(1 << L), true, false>(jb, idx, b0, b1, r0, r1, R, sh, o); \
+      else small_job<(1 << L), false, false>(jb, idx, b0, b1, r0, r1, R, sh, o); \
+    } \
     break;
   switch(jb.wc_log2){
     ODP_SMALL_CASE(1) ODP_SMALL_CASE(2) ODP_SMALL_CASE(3) ODP_SMALL_CASE(4)
@@ -1139,7 +1200,7 @@ int gbx_small_clusters(int cluster, int threads, size_t smem_bytes, int *active)
 }
 
 int gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, const gbx_expand_desc *desc0,
-                     gbx_small_rec *rec, size_t smem_bytes, int cluster, int threads, void *stream)
+                     gbx_small_rec *rec, size_t smem_bytes, int cluster, int threads, int part, void *stream)
 {
   if(njobs <= 0) return 0;
   if(!small_shape_ok(cluster, threads, smem_bytes) || (!descs && !desc0)) return (int)cudaErrorInvalidValue;
@@ -1148,7 +1209,7 @@ int gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *de
   gbx_expand_desc d0;
   if(desc0) d0 = *desc0;
   else memset(&d0, 0, sizeof(d0));
-  return (int)cudaLaunchKernelEx(&cfg, small_kernel, d_jobs, descs, rec, d0);
+  return (int)cudaLaunchKernelEx(&cfg, small_kernel, d_jobs, descs, rec, d0, part ? 1 : 0);
 }
 
 int gbx_host_device_ptr(void *host, void **dev)

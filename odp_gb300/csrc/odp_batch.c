@@ -100,11 +100,12 @@ int ODPX_Batch_info(const ODPX_Batch *batch, int graph, int *njobs, int *nslots,
 
 int ODPX_Batch_kernel(const ODPX_Batch *batch) { return batch ? batch->small : ODPX_ERR_INVALID; }
 
-int ODPX_Batch_small_shape(const ODPX_Batch *batch, int *cluster, int *threads)
+int ODPX_Batch_small_shape(const ODPX_Batch *batch, int *cluster, int *threads, int *partitioned)
 {
   if(!batch || !batch->small) return ODPX_ERR_INVALID;
   if(cluster) *cluster = batch->small_cluster;
   if(threads) *threads = batch->small_threads;
+  if(partitioned) *partitioned = batch->small_part;
   return 0;
 }
 

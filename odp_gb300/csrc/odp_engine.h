@@ -166,9 +166,11 @@ typedef struct {
  * shared memory; the job's record goes to rec[job].  `descs` and `rec` are
  * device addresses of pinned host memory (gbx_host_device_ptr).  With
  * `descs` NULL every job belongs to graph 0, whose descriptor `*desc0` is
- * passed by value in the launch's parameters (no host-memory read for it). */
+ * passed by value in the launch's parameters (no host-memory read for it).
+ * With `part` set each CTA holds only its own rows of the bitset buffers
+ * (1/cluster of them) and gathers the others' rows from their shared memory. */
 int  gbx_small_launch(const gbx_job *d_jobs, int njobs, const gbx_expand_desc *descs, const gbx_expand_desc *desc0,
-                      gbx_small_rec *rec, size_t smem_bytes, int cluster, int threads, void *stream);
+                      gbx_small_rec *rec, size_t smem_bytes, int cluster, int threads, int part, void *stream);
 /* How many clusters of that shape the GPU holds at once (0: the shape does
  * not fit; then it cannot be launched). */
 int  gbx_small_clusters(int cluster, int threads, size_t smem_bytes, int *active);

@@ -57,28 +57,32 @@ void odp_tuning_defaults(odp_tuning *t, int batch)
   t->direct = env_int("ODP_GB300_DIRECT", 1);
   t->small_n = env_int("ODP_GB300_SMALL_N", 8192);
   t->small_cluster = env_int("ODP_GB300_SMALL_CLUSTER", 0);
+  t->small_part = env_int("ODP_GB300_SMALL_PART", -1);
 }
 
 /* Chunk width (log2 words) for a graph whose whole level runs in shared
  * memory on a cluster of `cluster` CTAs: the widest of at most 16 words, and
  * at most the graph's own width, whose two bitset buffers (whole in every
- * CTA) and row table (1/cluster of the rows per CTA) fit; 0 if none does. */
-static int small_wc_log2(int n, int dp, int full_l2, int cluster)
+ * CTA, or with `part` only the CTA's rows) and row table (1/cluster of the
+ * rows per CTA) fit; 0 if none does. */
+static int small_wc_log2(int n, int dp, int full_l2, int cluster, int part)
 {
   const size_t rows = (size_t)(n + cluster - 1) / (size_t)cluster;
+  const size_t buf_rows = part ? rows : (size_t)n;
   for(int wl = full_l2 < 4 ? full_l2 : 4; wl >= 1; wl--){
-    size_t bytes = 2 * (size_t)n * ((size_t)8 << wl) + rows * (size_t)dp * 4;
+    size_t bytes = 2 * buf_rows * ((size_t)8 << wl) + rows * (size_t)dp * 4;
     if(bytes <= GBX_SMALL_SMEM_MAX) return wl;
   }
   return 0;
 }
 
 /* Shared memory per CTA of the small kernel when `cluster` CTAs share a job:
- * both bitset buffers whole, the row table of 1/cluster of the rows. */
-static size_t small_bytes(int n, int dp, int wl, int cluster)
+ * both bitset buffers (whole, or with `part` the CTA's 1/cluster of the
+ * rows) and the row table of 1/cluster of the rows. */
+static size_t small_bytes(int n, int dp, int wl, int cluster, int part)
 {
   const size_t rows = (size_t)(n + cluster - 1) / (size_t)cluster;
-  return 2 * (size_t)n * ((size_t)8 << wl) + rows * (size_t)dp * 4;
+  return 2 * (part ? rows : (size_t)n) * ((size_t)8 << wl) + rows * (size_t)dp * 4;
 }
 
 /* Threads per CTA for a CTA's rows: one lane per 16 bytes of a row (at most
@@ -313,10 +317,20 @@ static long long small_job_count(const odp_shape *shapes, int count, const int *
  * clusters of 8, two waves) took 151 and 257 us in the small kernel against
  * 84 and 95 us in the engine, while one-wave graphs up to n = 4096 gained
  * (n = 4096, d = 8: 55 against 85 us; a 64 x 64 grid: 176 against 418 us).
- * A cluster size forced by ODP_GB300_SMALL_CLUSTER is used if the graphs fit
- * at it (else halved), whatever the SM count. */
+ * The replicated layout (every CTA holds the whole level) is tried first.
+ * Plans of grid graphs whose whole level does not fit in one CTA take the
+ * partitioned layout (each CTA holds its rows, neighbour rows are read from
+ * the CTA that owns them through distributed shared memory), which fits
+ * graphs up to `cluster` times larger.  Its gathers run at about one 16-byte
+ * request per clock per SM, so it pays only where levels are many and
+ * light: on GB300, grids of n = 5184, 6400 and 8100 (diameters 49 to 74)
+ * took 265, 301 and 655 us against 547, 626 and 888 us in the engine, while
+ * general graphs lost (n = 8192, d = 8: 339 against 122 us; n = 4096,
+ * d = 24: 304 against 83 us).  A cluster size forced by
+ * ODP_GB300_SMALL_CLUSTER is used if the graphs fit at it (else halved),
+ * whatever the SM count; ODP_GB300_SMALL_PART=0 or 1 forces the layout. */
 static int choose_small(const odp_shape *shapes, int count, const odp_tuning *t, int sms, int *wl,
-                        int *cluster_out, int *threads_out, size_t *smem_out)
+                        int *cluster_out, int *threads_out, size_t *smem_out, int *part_out)
 {
   if(count <= 0 || t->small_n <= 0 || t->wc_log2 > 0 || t->slots > 0 || t->tile_rows > 0 || t->local_kb_explicit)
     return 0;
@@ -328,12 +342,16 @@ static int choose_small(const odp_shape *shapes, int count, const odp_tuning *t,
   }
   if(gbx_small_prepare()) return 0;
   const int want = t->small_cluster > 0 && t->small_cluster <= GBX_SMALL_CLUSTER_MAX ? t->small_cluster : 0;
-  {
+  int all_grids = 1;
+  for(int i = 0; i < count; i++) all_grids &= shapes[i].grid != 0;
+  for(int part = t->small_part > 0 ? 1 : 0; part <= (t->small_part == 0 ? 0 : 1); part++){
     for(int c = want ? want : GBX_SMALL_CLUSTER_MAX; c >= 1; c >>= 1){
+      if(part && c == 1) continue;                 /* one CTA: the replicated layout */
+      if(part && t->small_part < 0 && !all_grids) continue;
       int ok = 1;
       for(int i = 0; i < count && ok; i++){
         const int W = shape_words(&shapes[i]);
-        wl[i] = small_wc_log2(shape_n(&shapes[i]), shape_dp(&shapes[i]), ilog2_ceil(W < 2 ? 2 : W), c);
+        wl[i] = small_wc_log2(shape_n(&shapes[i]), shape_dp(&shapes[i]), ilog2_ceil(W < 2 ? 2 : W), c, part);
         if(!wl[i]) ok = 0;
       }
       if(!ok) continue;
@@ -352,7 +370,7 @@ static int choose_small(const odp_shape *shapes, int count, const odp_tuning *t,
       size_t smem = 0;
       int threads = 64;
       for(int i = 0; i < count; i++){
-        const size_t b = small_bytes(shape_n(&shapes[i]), shape_dp(&shapes[i]), wl[i], c);
+        const size_t b = small_bytes(shape_n(&shapes[i]), shape_dp(&shapes[i]), wl[i], c, part);
         const int th = small_threads_for(shape_n(&shapes[i]), wl[i], c);
         if(b > smem) smem = b;
         if(th > threads) threads = th;
@@ -362,6 +380,7 @@ static int choose_small(const odp_shape *shapes, int count, const odp_tuning *t,
         *cluster_out = c;
         *threads_out = threads;
         *smem_out = smem;
+        *part_out = part;
         return 1;
       }
     }
@@ -398,7 +417,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   const int sms = g_sm_count > 0 ? g_sm_count : 1;
   int *small_wl = calloc((size_t)count, sizeof(int));
   int small = choose_small(shapes, count, tuning, sms, small_wl, &p->small_cluster, &p->small_threads,
-                           &p->small_smem);
+                           &p->small_smem, &p->small_part);
 
   /* Shapes, chunk widths, tiles. */
   int njobs = 0;
@@ -703,7 +722,8 @@ int odp_plan_enqueue_engine(odp_plan *p)
      * the launch's parameters, so the plan is launched directly each call */
     const int one = p->ngraphs == 1;
     return gbx_small_launch(p->d_jobs, p->njobs, one ? NULL : p->d_small_desc, one ? &p->h_expand[0] : NULL,
-                            p->d_small_rec, p->small_smem, p->small_cluster, p->small_threads, p->stream);
+                            p->d_small_rec, p->small_smem, p->small_cluster, p->small_threads, p->small_part,
+                            p->stream);
   }
   return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
                            (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),

@@ -34,6 +34,7 @@ typedef struct {
   int direct;                  /* pull callers' adjacency from host memory when the device can (1, default) */
   int small_n;                 /* graphs of at most this many vertices may run in shared memory (0: never) */
   int small_cluster;           /* CTAs per small-kernel job: 1, 2, 4 or 8; 0 = automatic */
+  int small_part;              /* small-kernel rows partitioned over the cluster: -1 when needed, 0 never, 1 always */
 } odp_tuning;
 
 typedef struct {
@@ -77,6 +78,7 @@ typedef struct odp_plan {
   size_t small_smem;           /* shared memory per CTA of the small-graph kernel */
   int small_cluster;           /* CTAs (one thread-block cluster) per job of the small-graph kernel */
   int small_threads;           /* threads per CTA of the small-graph kernel */
+  int small_part;              /* 1: each CTA holds only its rows of the bitsets (partitioned layout) */
   gbx_small_rec *h_small_rec;  /* small plans: per-job records, pinned; the kernel writes them */
   gbx_small_rec *d_small_rec;  /*   the same memory, as the device addresses it */
   gbx_expand_desc *d_small_desc; /* small plans: h_expand as the device addresses it */

@@ -237,24 +237,27 @@ def test_small_graph_kernel_and_engine_agree(small_n, monkeypatch):
         assert b.kernel() == kernel
         assert same(b.run()[0], y)
         b.close()
-    big = og.GraphSpec(g(8192, 8, seed=14), nodes=8192)                 # one graph too large mixes in: engine
+    big = og.GraphSpec(g(16384, 8, seed=14), nodes=16384)               # one graph too large mixes in: engine
     b = og.Batch(cases[:2] + [big])
     assert b.kernel() == "engine"
     b.close()
 
 
-@pytest.mark.parametrize("cluster", [1, 2, 4, 8])
-def test_small_kernel_cluster_sizes(cluster, monkeypatch):
+@pytest.mark.parametrize("cluster,part", [(1, 0), (2, 0), (4, 0), (8, 0), (2, 1), (4, 1), (8, 1)])
+def test_small_kernel_cluster_sizes(cluster, part, monkeypatch):
     """A small-kernel job runs on the CTAs of one thread-block cluster: each
     CTA computes its share of the rows and stores them into every CTA's copy
     of the level (distributed shared memory), and each builds the row-table
     entries of 1/cluster of the adjacency for the CTAs that own the rows.
-    Forced cluster sizes of 1 to 8 CTAs give the oracle's results on row
+    In the partitioned layout each CTA holds only its own rows and gathers
+    the others' from their shared memory.  Forced cluster sizes of 1 to 8
+    CTAs, in both layouts, give the oracle's results on row
     counts that do not divide evenly (n = 998, 1000) or are below the
     cluster size (n = 5, 6), symmetric general and grid graphs (rows placed
     through the rotation table), irregular and disconnected graphs, and the
     n = 1024 golden graph, one plan per graph and as one plan."""
     monkeypatch.setenv("ODP_GB300_SMALL_CLUSTER", str(cluster))
+    monkeypatch.setenv("ODP_GB300_SMALL_PART", str(part))
     g = lambda n, d, s=1, seed=1: og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, s, seed=seed), d, s)
     cases = _saturation_cases()
     cases += [og.GraphSpec(g(n, d, seed=20 + n), nodes=n) for n, d in ((998, 3), (1000, 6), (6, 3), (5, 4), (1024, 8))]
@@ -267,32 +270,37 @@ def test_small_kernel_cluster_sizes(cluster, monkeypatch):
     for k, (c, y) in enumerate(zip(cases, refs)):
         b = og.Batch([c])
         assert b.kernel() == "small"
-        assert b.small_shape()[0] == cluster
-        assert same(b.run()[0], y), (k, cluster)
-        assert same(b.run()[0], y), (k, cluster)
+        assert b.small_shape()[0] == cluster and b.small_shape()[2] == part
+        assert same(b.run()[0], y), (k, cluster, part)
+        assert same(b.run()[0], y), (k, cluster, part)
         b.close()
     b = og.Batch(cases)
-    assert b.kernel() == "small" and b.small_shape()[0] == cluster
+    assert b.kernel() == "small" and b.small_shape()[0] == cluster and b.small_shape()[2] == part
     for k, (x, y) in enumerate(zip(b.run(), refs)):
-        assert same(x, y), (k, cluster)
+        assert same(x, y), (k, cluster, part)
     b.close()
     monkeypatch.delenv("ODP_GB300_SMALL_CLUSTER")
+    monkeypatch.delenv("ODP_GB300_SMALL_PART")
     b = og.Batch([cases[-3]])                                  # n = 1024, d = 8: 8 jobs on clusters of 8
-    assert b.small_shape()[0] == 8
+    assert b.small_shape()[:3:2] == (8, 0)
     b.close()
 
 
 def test_small_kernel_mid_size_graphs():
     """With the row table split over a cluster, graphs up to n = 4096 whose
     bitset buffers fit run in the small kernel when their jobs fit on the SMs
-    in one wave; a graph that would need two waves runs in the engine.  Both
+    in one wave; larger grids (90 x 90) with the rows partitioned over the
+    cluster; general graphs that would need two waves run in the engine.  All
     give the oracle's results."""
     g = lambda n, d, seed: og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=seed), d)
     e = og.generate_random_grid(64, 64, 6, 3, 1, seed=3)
+    e90 = og.generate_random_grid(90, 90, 4, 3, 1, seed=4)
     cases = [(og.GraphSpec(g(3000, 16, 31), nodes=3000), "small"),
              (og.GraphSpec(g(4096, 8, 32), nodes=4096), "small"),
              (og.GraphSpec(og.conv_edge2adjacency_grid(64, 64, e, 6, 1), grid=True, width=64, height=64), "small"),
-             (og.GraphSpec(g(4096, 24, 33), nodes=4096), "engine")]
+             (og.GraphSpec(og.conv_edge2adjacency_grid(90, 90, e90, 4, 1), grid=True, width=90, height=90), "small"),
+             (og.GraphSpec(g(4096, 24, 33), nodes=4096), "engine"),
+             (og.GraphSpec(g(8192, 8, 34), nodes=8192), "engine")]
     for c, kernel in cases:
         want = oracle.aspl(c.adjacency, nodes=c.nodes, grid=c.grid, width=c.width, height=c.height)
         b = og.Batch([c])
