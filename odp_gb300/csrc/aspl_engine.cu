@@ -141,10 +141,25 @@ __device__ __forceinline__ int expand_value(const gbx_expand_desc &e, int a, int
 
 /* One descriptor per blockIdx.y: its compact adjacency, read from host
  * memory by consecutive threads in 16-byte pieces when both ends are 16-byte
- * aligned, else in 4-byte pieces. */
-__global__ void pull_kernel(const gbx_expand_desc *__restrict__ descs)
+ * aligned, else in 4-byte pieces.  The descriptors come from pinned host
+ * memory (`hdescs`: this call's adjacency pointers); block (0, y) stores
+ * descriptor y into `ddescs` for expand_kernel.  All blocks together also
+ * copy the plan's initial engine state (`state_init`, `state_words` 8-byte
+ * words, device memory) over `state`. */
+__global__ void pull_kernel(const gbx_expand_desc *hdescs, gbx_expand_desc *ddescs,
+                            unsigned long long *__restrict__ state, const unsigned long long *__restrict__ state_init,
+                            long long state_words)
 {
-  const gbx_expand_desc &e = descs[blockIdx.y];
+  __shared__ gbx_expand_desc s_desc;
+  const long long nthreads = (long long)gridDim.x * gridDim.y * blockDim.x;
+  const long long tid = ((long long)blockIdx.y * gridDim.x + blockIdx.x) * blockDim.x + threadIdx.x;
+  for(long long i = tid; i < state_words; i += nthreads) state[i] = state_init[i];
+  if(threadIdx.x == 0){
+    s_desc = hdescs[blockIdx.y];
+    if(blockIdx.x == 0) ddescs[blockIdx.y] = s_desc;
+  }
+  __syncthreads();
+  const gbx_expand_desc &e = s_desc;
   if(!e.adj_dev) return;
   const long long ints = (long long)(e.n / e.s) * e.d;
   const long long stride = (long long)gridDim.x * blockDim.x;
@@ -161,9 +176,15 @@ __global__ void pull_kernel(const gbx_expand_desc *__restrict__ descs)
   }
 }
 
+#define EXPAND_GROUP 8         /* neighbour entries per thread, loaded before any is stored */
+
+/* Thread (global vertex gv, group blockIdx.y) writes entries [8y, 8y + 8)
+ * of gv's row of its graph's neighbour table: all eight compact-adjacency
+ * loads are issued before the first store. */
 __global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int ndesc, long long total,
                               unsigned int *err)
 {
+  const int j0 = (int)blockIdx.y * EXPAND_GROUP;
   for(long long gv = blockIdx.x * (long long)blockDim.x + threadIdx.x; gv < total;
       gv += (long long)gridDim.x * blockDim.x){
     int lo = 0, hi = ndesc - 1;
@@ -172,9 +193,10 @@ __global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int nde
       if(descs[mid].first_vertex <= gv) lo = mid; else hi = mid - 1;
     }
     const gbx_expand_desc &e = descs[lo];
+    const int d = e.d, dp = e.dp;
+    if(j0 >= dp) continue;
     const int *adj = e.adj_dev ? e.adj_dev : e.adj;
     const int v = (int)(gv - e.first_vertex);
-    const int d = e.d, dp = e.dp;
     bool bad = false;
     int deg = e.ndeg ? e.ndeg[v] : d;
     if(deg < 0 || deg > d){ bad = true; deg = deg < 0 ? 0 : d; }
@@ -183,10 +205,17 @@ __global__ void expand_kernel(const gbx_expand_desc *__restrict__ descs, int nde
     /* Entries that are not neighbours (beyond the vertex's degree, padding,
      * or out of range, which is also reported) hold the row itself: OR-ing a
      * row into itself changes nothing, so the gather needs no test. */
-    for(int j = 0; j < dp; j++){
-      int back = 0;
-      const int a = j < deg ? adj[entry_source(e, v, j, back)] : 0;
-      out[j] = expand_value(e, a, back, j, deg, row, bad);
+    int val[EXPAND_GROUP], back[EXPAND_GROUP];
+#pragma unroll
+    for(int k = 0; k < EXPAND_GROUP; k++){
+      const int j = j0 + k;
+      back[k] = 0;
+      val[k] = j < deg ? adj[entry_source(e, v, j, back[k])] : 0;
+    }
+#pragma unroll
+    for(int k = 0; k < EXPAND_GROUP; k++){
+      const int j = j0 + k;
+      if(j < dp) out[j] = expand_value(e, val[k], back[k], j, deg, row, bad);
     }
     if(bad) atomicOr(err, GBX_ERR_BAD_ADJ);
   }
@@ -1217,20 +1246,27 @@ int gbx_host_device_ptr(void *host, void **dev)
   return (int)cudaHostGetDevicePointer(dev, host, 0);
 }
 
-int gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream)
+int gbx_pull(const gbx_expand_desc *h_descs, gbx_expand_desc *d_descs, int ndesc, void *d_state,
+             const void *d_state_init, size_t state_bytes, void *stream)
 {
   if(ndesc <= 0) return 0;
-  pull_kernel<<<dim3(32, (unsigned)ndesc), 256, 0, (cudaStream_t)stream>>>(d_descs);
+  if(state_bytes % 8) return (int)cudaErrorInvalidValue;
+  pull_kernel<<<dim3(32, (unsigned)ndesc), 256, 0, (cudaStream_t)stream>>>(
+      h_descs, d_descs, (unsigned long long *)d_state, (const unsigned long long *)d_state_init,
+      (long long)(state_bytes / 8));
   return (int)cudaGetLastError();
 }
 
-int gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices, unsigned int *d_error,
+int gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices, int max_dp, unsigned int *d_error,
                void *stream)
 {
   if(total_vertices <= 0) return 0;
+  if(max_dp <= 0 || max_dp > 65535 * EXPAND_GROUP) return (int)cudaErrorInvalidValue;
   long long blocks = (total_vertices + 255) / 256;
   if(blocks > 65535LL * 8) blocks = 65535LL * 8;
-  expand_kernel<<<(unsigned)blocks, 256, 0, (cudaStream_t)stream>>>(d_descs, ndesc, total_vertices, d_error);
+  const unsigned groups = (unsigned)((max_dp + EXPAND_GROUP - 1) / EXPAND_GROUP);
+  expand_kernel<<<dim3((unsigned)blocks, groups), 256, 0, (cudaStream_t)stream>>>(d_descs, ndesc, total_vertices,
+                                                                                d_error);
   return (int)cudaGetLastError();
 }
 
@@ -1483,7 +1519,8 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   unsigned int *d_err = (unsigned int *)(base + off_state + out_off + sizeof(gbx_ctrl));
   long long eblocks = ((long long)n + 255) / 256;
   if(eblocks > 65535LL * 8) eblocks = 65535LL * 8;
-  expand_kernel<<<(unsigned)eblocks, 256, 0, st>>>((const gbx_expand_desc *)(base + off_desc), 1, n, d_err);
+  expand_kernel<<<dim3((unsigned)eblocks, (unsigned)((desc.dp + EXPAND_GROUP - 1) / EXPAND_GROUP)), 256, 0, st>>>(
+      (const gbx_expand_desc *)(base + off_desc), 1, n, d_err);
   engine_kernel<<<nd->blocks, ENGINE_THREADS, STAGE_BYTES_PLAIN, st>>>(
       (const gbx_job *)(base + off_jobs), njobs, (gbx_slot *)(base + off_state), nslots,
       (gbx_ctrl *)(base + off_state + out_off), (gbx_graph_acc *)(base + off_state + acc_off),

@@ -133,7 +133,7 @@ int  gbx_stream_sync(void *stream);
 const char *gbx_error_string(int err);
 
 /* Kernels. */
-int  gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices,
+int  gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices, int max_dp,
                 unsigned int *d_error, void *stream);
 int  gbx_engine_blocks(int active);
 /* 1 when kernels can read pageable host memory directly (after gbx_device_init). */
@@ -145,8 +145,13 @@ int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int 
                        unsigned long long spin_limit_ns, int blocks, int active, void *stream);
 
 /* Copies every descriptor's host array `adj` into its `adj_dev` with
- * coalesced 16-byte loads over the CPU-GPU link (pageable host memory). */
-int  gbx_pull(const gbx_expand_desc *d_descs, int ndesc, void *stream);
+ * coalesced 16-byte loads over the CPU-GPU link (pageable host memory).  The
+ * descriptors are read from pinned host memory (`h_descs`, a device address)
+ * and stored into `d_descs` for gbx_expand; the same launch copies the
+ * initial engine state `d_state_init` over `d_state` (state_bytes, a multiple
+ * of 8), so a call needs no separate uploads for either. */
+int  gbx_pull(const gbx_expand_desc *h_descs, gbx_expand_desc *d_descs, int ndesc, void *d_state,
+              const void *d_state_init, size_t state_bytes, void *stream);
 /* Outcome of one job of the small-graph kernel, written to pinned host
  * memory: its last level (negative: stalled), error bits (GBX_ERR_*), its
  * share of the graph's ordered distance sum, and %globaltimer stamps. */

@@ -428,6 +428,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     g->n = sh->grid ? sh->width * sh->height : sh->nodes;
     g->d = sh->degree;
     g->dp = ALIGN_UP(sh->degree > 0 ? sh->degree : 1, 4);
+    if(g->dp > p->max_dp) p->max_dp = g->dp;
     g->s = sh->symmetries;
     g->grid_s = sh->grid && sh->symmetries != 1;
     g->width = sh->width;
@@ -611,6 +612,12 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
     CK(gbx_host_device_ptr(p->h_small_rec, (void **)&p->d_small_rec));
     CK(gbx_host_device_ptr(p->h_expand, (void **)&p->d_small_desc));
   }
+  else if(p->direct){
+    /* the pull kernel reads this call's descriptors from pinned memory and
+     * resets the engine state from a device copy of its initial value */
+    CK(gbx_host_device_ptr(p->h_expand, (void **)&p->d_hexpand));
+    CK(gbx_malloc((void **)&p->d_state_init, p->state_bytes));
+  }
   CK(gbx_host_alloc((void **)&p->h_state_init, p->state_bytes));
   CK(gbx_host_alloc((void **)&p->h_state_out, p->out_bytes));
 
@@ -671,6 +678,10 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   }
 
   fill_state_init(p);
+  if(p->d_state_init){
+    CK(gbx_memcpy_h2d(p->d_state_init, p->h_state_init, p->state_bytes, p->stream));
+    CK(gbx_stream_sync(p->stream));
+  }
   *out = p;
   return 0;
 
@@ -685,6 +696,7 @@ void odp_plan_destroy(odp_plan *p)
   if(p->graph_exec) gbx_graph_destroy(p->graph_exec);
   gbx_free(p->d_adj); gbx_free(p->d_ndeg); gbx_free(p->d_itable); gbx_free(p->d_nbr);
   gbx_free(p->d_slotbuf); gbx_free(p->d_slotmask); gbx_free(p->d_srcpos); gbx_free(p->d_expand); gbx_free(p->d_jobs); gbx_free(p->d_state);
+  gbx_free(p->d_state_init);
   gbx_host_free(p->h_adj); gbx_host_free(p->h_expand); gbx_host_free(p->h_state_init); gbx_host_free(p->h_state_out);
   gbx_host_free(p->h_small_rec);
   if(p->stream) gbx_stream_destroy(p->stream);
@@ -700,16 +712,17 @@ static int enqueue(odp_plan *p)
   int e;
   if(p->small) return odp_plan_enqueue_engine(p);
   if(p->direct){
-    /* the descriptors carry this call's host pointers; the pull kernel copies
-     * the arrays into the device copy that expand reads */
-    if((e = gbx_memcpy_h2d(p->d_expand, p->h_expand, sizeof(gbx_expand_desc) * (size_t)p->ngraphs, p->stream)))
+    /* one kernel: this call's descriptors (their host pointers) from pinned
+     * memory, the callers' arrays into the device copy that expand reads,
+     * and the engine state reset */
+    if((e = gbx_pull(p->d_hexpand, p->d_expand, p->ngraphs, p->d_state, p->d_state_init, p->state_bytes, p->stream)))
       return e;
-    if((e = gbx_pull(p->d_expand, p->ngraphs, p->stream))) return e;
   }
-  else if((e = gbx_memcpy_h2d(p->d_adj, p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4), p->stream)))
-    return e;
-  if((e = gbx_memcpy_h2d(p->d_state, p->h_state_init, p->state_bytes, p->stream))) return e;
-  if((e = gbx_expand(p->d_expand, p->ngraphs, p->total_vertices,
+  else{
+    if((e = gbx_memcpy_h2d(p->d_adj, p->h_adj, sizeof(int) * (p->adj_ints ? p->adj_ints : 4), p->stream))) return e;
+    if((e = gbx_memcpy_h2d(p->d_state, p->h_state_init, p->state_bytes, p->stream))) return e;
+  }
+  if((e = gbx_expand(p->d_expand, p->ngraphs, p->total_vertices, p->max_dp,
                      (unsigned int *)(p->d_state + p->out_off + sizeof(gbx_ctrl)), p->stream))) return e;
   if((e = odp_plan_enqueue_engine(p))) return e;
   return gbx_memcpy_d2h(p->h_state_out, p->d_state + p->out_off, p->out_bytes, p->stream);
@@ -852,6 +865,8 @@ static int reorder_by_duration(odp_plan *p)
   free(ord); free(nj); free(no);
   fill_state_init(p);
   if(gbx_memcpy_h2d(p->d_jobs, p->h_jobs, sizeof(gbx_job) * (size_t)p->njobs, p->stream)) return ODPX_ERR_CUDA;
+  if(p->d_state_init && gbx_memcpy_h2d(p->d_state_init, p->h_state_init, p->state_bytes, p->stream))
+    return ODPX_ERR_CUDA;
   if(gbx_stream_sync(p->stream)) return ODPX_ERR_CUDA;
   return 0;
 }

@@ -79,6 +79,9 @@ typedef struct odp_plan {
   int small_cluster;           /* CTAs (one thread-block cluster) per job of the small-graph kernel */
   int small_threads;           /* threads per CTA of the small-graph kernel */
   int small_part;              /* 1: each CTA holds only its rows of the bitsets (partitioned layout) */
+  int max_dp;                  /* widest neighbour-table row of the plan */
+  gbx_expand_desc *d_hexpand;  /* device address of h_expand (direct engine plans) */
+  char *d_state_init;          /* device copy of h_state_init (direct engine plans) */
   gbx_small_rec *h_small_rec;  /* small plans: per-job records, pinned; the kernel writes them */
   gbx_small_rec *d_small_rec;  /*   the same memory, as the device addresses it */
   gbx_expand_desc *d_small_desc; /* small plans: h_expand as the device addresses it */

@@ -559,7 +559,7 @@ int ODPX_Serve_register(ODPX_Server *s, const ODP_Graph *gr, int *handle)
   e |= gbx_memset(d_err, 0, sizeof(unsigned), s->ctl_stream);
   e |= gbx_memcpy_h2d(g.d_adj, gr->adjacency, sizeof(int) * adj_ints, s->ctl_stream);
   e |= gbx_memcpy_h2d(g.d_desc, &desc, sizeof(desc), s->ctl_stream);
-  e |= gbx_expand(g.d_desc, 1, n, d_err, s->ctl_stream);
+  e |= gbx_expand(g.d_desc, 1, n, g.dp, d_err, s->ctl_stream);
   e |= gbx_memcpy_d2h(&h_err, d_err, sizeof(unsigned), s->ctl_stream);
   e |= gbx_stream_sync(s->ctl_stream);
   gbx_free(d_err);
