@@ -137,6 +137,58 @@ def test_batch_matches_single_and_oracle(golden):
     assert all(same(a, b) for a, b in zip(got, got2))
 
 
+def test_engine_batch_with_new_arrays_and_a_bad_entry(golden, monkeypatch):
+    """A batch on the engine (general, symmetric, grid, non-regular,
+    directed and disconnected graphs): each call's pull kernel reads the
+    descriptors of that call from pinned memory, copies the callers' arrays
+    and resets the engine state, so a second call with other arrays of the
+    same shapes gives their results, an out-of-range entry in any graph is
+    reported, and the next call is right again."""
+    monkeypatch.setenv("ODP_GB300_SMALL_N", "0")
+    rng = np.random.default_rng(17)
+    specs, kws = [], []
+    for _ in range(44):
+        spec, kw = random_graph(rng)
+        specs.append(spec)
+        kws.append(kw)
+    for c in golden["cases"]:        # non-regular, directed, disconnected, tiny graphs
+        if c["kind"] == "general":
+            specs.append(og.GraphSpec(case_adjacency(c), nodes=c["nodes"], symmetries=c["symmetries"],
+                                      num_degrees=case_degrees(c)))
+            kws.append(dict(nodes=c["nodes"], symmetries=c["symmetries"], num_degrees=case_degrees(c)))
+    assert len(specs) >= 32
+    refs = [oracle.aspl(sp.adjacency, **kw) for sp, kw in zip(specs, kws)]
+    got = og.set_aspl_batch(specs)
+    for k, (g, r) in enumerate(zip(got, refs)):
+        assert same(g, r), (k, kws[k])
+    # same shapes, other arrays: the graphs of equal shape swapped
+    swapped = list(specs)
+    for i in range(len(specs)):
+        for j in range(i + 1, len(specs)):
+            a, b = specs[i], specs[j]
+            if (a.grid, a.nodes, a.width, a.height, a.degree, a.symmetries) == \
+               (b.grid, b.nodes, b.width, b.height, b.degree, b.symmetries) and a.num_degrees is None \
+               and b.num_degrees is None and swapped[i] is a and swapped[j] is b:
+                swapped[i] = og.GraphSpec(b.adjacency, grid=a.grid, nodes=a.nodes, width=a.width, height=a.height,
+                                          symmetries=a.symmetries)
+                swapped[j] = og.GraphSpec(a.adjacency, grid=b.grid, nodes=b.nodes, width=b.width, height=b.height,
+                                          symmetries=b.symmetries)
+    want = []
+    for sp in swapped:
+        k = next(i for i, x in enumerate(specs) if x.adjacency is sp.adjacency)
+        want.append(refs[k])
+    for k, (g, r) in enumerate(zip(og.set_aspl_batch(swapped), want)):
+        assert same(g, r), k
+    bad = [og.GraphSpec(sp.adjacency.copy(), grid=sp.grid, nodes=sp.nodes, width=sp.width, height=sp.height,
+                        symmetries=sp.symmetries, num_degrees=sp.num_degrees) for sp in specs]
+    bad[len(bad) // 2].adjacency[0, 0] = 1 << 20
+    with pytest.raises(og.ODPError) as ei:
+        og.set_aspl_batch(bad)
+    assert ei.value.code == og.ERR_ADJACENCY
+    for g, r in zip(og.set_aspl_batch(specs), refs):
+        assert same(g, r)
+
+
 def test_batch_plan_reuse_with_new_adjacency():
     n, d = 512, 6
     adjs = [og.conv_edge2adjacency_general(n, og.generate_random_general(n, d, seed=s), d) for s in range(8)]
