@@ -664,7 +664,7 @@ def run_own(args):
         autotune.apply(tune_report)
         tune_report = dict(tune_report, loaded_from=args.tuning_file)
     else:
-        tune_report = autotune.tune_batch(specs) if not args.no_tune else None
+        tune_report = autotune.tune_batch_best(specs) if not args.no_tune else None
     if args.save_tuning and tune_report is not None:
         with open(args.save_tuning, "w") as f:
             json.dump(tune_report, f)

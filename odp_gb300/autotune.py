@@ -126,6 +126,26 @@ def tune_batch(specs, slots=(32, 64, 128), local_kb=(256, 2048), widths=(3, 4, 5
             "seconds": time.perf_counter() - t0}
 
 
+def tune_batch_best(specs, starts=2, repeats=10, **kw):
+    """Runs tune_batch `starts` times and keeps the schedule that measures
+    fastest over `repeats` further runs.  The greedy search ends at different
+    schedules from one run to the next (on GB300, the 512-graph batch has
+    ended anywhere from 6.86 to 7.17 ms), so the best of two is steadier than
+    one.  Installs and returns the kept report, with every start's time."""
+    best, times = None, []
+    for _ in range(starts):
+        r = tune_batch(specs, **kw)
+        ms = measure(specs, repeats)
+        times.append(ms)
+        if best is None or ms < best[0]:
+            best = (ms, r)
+    apply(best[1])
+    rep = dict(best[1])
+    rep["tuned_ms"] = best[0]
+    rep["starts_ms"] = times
+    return rep
+
+
 def tune_single(spec, widths=(3, 4, 5, 6), slots=(2, 4, 8, 16, 32), tile_kb=(128, 288, 640), repeats=3):
     """Tunes one graph's bucket (chunk width, tile traffic) and the slots."""
     clear()
