@@ -234,11 +234,23 @@ struct RowShape {
   static constexpr int RPW = 32 / G;                 /* rows per warp pass */
 };
 
-/* Set local source bit b (0 <= b < nsrc) if it lands in this lane's vectors. */
+/* The shape of the change-tracking passes when every job of a plan tracks
+ * changes: half as many lanes per row, two vectors each, so a warp pass
+ * covers twice the rows.  Few neighbours of a row change per level, so a
+ * lane's gathers for one row are few; two rows per lane keep twice as many
+ * loads in flight with the same registers. */
 template <int WC>
-__device__ __forceinline__ void mark_source(uint4 (&acc)[RowShape<WC>::V], int b, int nsrc, int gl)
+struct RowShapeWide {
+  static constexpr int VPR = WC / 2;
+  static constexpr int G = VPR >= 64 ? 32 : (VPR >= 2 ? VPR / 2 : 1);
+  static constexpr int V = VPR / G;
+  static constexpr int RPW = 32 / G;
+};
+
+/* Set local source bit b (0 <= b < nsrc) if it lands in this lane's vectors. */
+template <class S>
+__device__ __forceinline__ void mark_source(uint4 (&acc)[S::V], int b, int nsrc, int gl)
 {
-  typedef RowShape<WC> S;
   if((unsigned)b >= (unsigned)nsrc) return;
   const int vec = b >> 7;
   const unsigned bit = 1u << (b & 31);
@@ -295,11 +307,10 @@ __device__ __forceinline__ int source_of(const int *srcpos, int row)
 
 /* Level 1: P_1[v] = {v} u N(v), restricted to the chunk's sources, and the
  * lanes of each row whose words differ from the identity P_0. */
-template <int WC, bool ACT, bool SP>
+template <int WC, bool ACT, bool SP, class S = RowShape<WC>>
 __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsigned long long *Y,
                                 unsigned *Mcur, int row0, int nrows)
 {
-  typedef RowShape<WC> S;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
   const int src0 = jb.src0, nsrc = jb.nsrc;
@@ -314,15 +325,15 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
 #pragma unroll
       for(int k = 0; k < S::V; k++){ acc[k] = make_uint4(0u, 0u, 0u, 0u); id[k] = acc[k]; }
       const int self = source_of<SP>(jb.srcpos, row) - src0;
-      mark_source<WC>(acc, self, nsrc, gl);
-      if(ACT) mark_source<WC>(id, self, nsrc, gl);
+      mark_source<S>(acc, self, nsrc, gl);
+      if(ACT) mark_source<S>(id, self, nsrc, gl);
       const int4 *ip = reinterpret_cast<const int4 *>(st.idx + r * dp);
       for(int j = 0; j < (dp >> 2); j++){
         int4 q = ip[j];
-        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.x) - src0, nsrc, gl);
-        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.y) - src0, nsrc, gl);
-        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.z) - src0, nsrc, gl);
-        mark_source<WC>(acc, source_of<SP>(jb.srcpos, q.w) - src0, nsrc, gl);
+        mark_source<S>(acc, source_of<SP>(jb.srcpos, q.x) - src0, nsrc, gl);
+        mark_source<S>(acc, source_of<SP>(jb.srcpos, q.y) - src0, nsrc, gl);
+        mark_source<S>(acc, source_of<SP>(jb.srcpos, q.z) - src0, nsrc, gl);
+        mark_source<S>(acc, source_of<SP>(jb.srcpos, q.w) - src0, nsrc, gl);
       }
       uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
       unsigned c = 0;
@@ -419,11 +430,10 @@ __device__ unsigned rows_levelk_all(Stage &st, int dp, int d, int nsrc, const un
  * its words differ from that (changed at k-1 or at k), except at level 2,
  * where Y has never been written and every word is stored.  Returns the bits
  * added at this level; the row's new change mask goes to Mcur. */
-template <int WC>
+template <int WC, class S = RowShape<WC>>
 __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long long *X, unsigned long long *Y,
                                 unsigned *Mcur, int row0, int nrows, bool write_all)
 {
-  typedef RowShape<WC> S;
   constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;       /* neighbours gathered per step */
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
@@ -479,15 +489,37 @@ __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long lon
   return cnt;
 }
 
-template <int WC>
+/* Engine instantiations by change tracking: MODE_ACTIVE compiles only the
+ * passes with it (plans whose every job tracks changes), MODE_MIXED both
+ * (every other plan).  An instantiation with only the passes without change
+ * tracking is not built: at the 64 registers of four CTAs per SM it spilled
+ * (60 bytes), where the one with both passes does not. */
+#define MODE_PLAIN 0
+#define MODE_ACTIVE 1
+#define MODE_MIXED 2
+
+template <int MODE>
+__device__ __forceinline__ bool job_active(const gbx_job &jb)
+{
+  return MODE == MODE_ACTIVE || (MODE == MODE_MIXED && (jb.flags & GBX_JOB_ACTIVE));
+}
+
+template <int WC, int MODE>
 __device__ unsigned run_block(Stage &st, int dp, const gbx_job &jb, int level, const unsigned long long *X,
                               unsigned long long *Y, unsigned *Mcur, int row0, int nrows)
 {
-  if(jb.flags & GBX_JOB_ACTIVE){
+  if(job_active<MODE>(jb)){
+    if(MODE == MODE_ACTIVE){
+      typedef RowShapeWide<WC> SW;
+      if(level > 1) return rows_levelk<WC, SW>(st, dp, X, Y, Mcur, row0, nrows, level == 2);
+      return jb.srcpos ? rows_level1<WC, true, true, SW>(st, dp, jb, Y, Mcur, row0, nrows)
+                       : rows_level1<WC, true, false, SW>(st, dp, jb, Y, Mcur, row0, nrows);
+    }
     if(level > 1) return rows_levelk<WC>(st, dp, X, Y, Mcur, row0, nrows, level == 2);
     return jb.srcpos ? rows_level1<WC, true, true>(st, dp, jb, Y, Mcur, row0, nrows)
                      : rows_level1<WC, true, false>(st, dp, jb, Y, Mcur, row0, nrows);
   }
+  if(MODE == MODE_ACTIVE) return 0;
   if(level > 1) return rows_levelk_all<WC>(st, dp, jb.d, jb.nsrc, X, Y, row0, nrows);
   return jb.srcpos ? rows_level1<WC, false, true>(st, dp, jb, Y, Mcur, row0, nrows)
                    : rows_level1<WC, false, false>(st, dp, jb, Y, Mcur, row0, nrows);
@@ -497,6 +529,7 @@ __device__ unsigned run_block(Stage &st, int dp, const gbx_job &jb, int level, c
  * lists (and, after level 1, the neighbours' and rows' change masks of the
  * previous level) in shared memory, then process the rows.  Returns this
  * thread's share of the level's count (level 1: bits set; later: added). */
+template <int MODE>
 __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsigned long long *X,
                              unsigned long long *Y, const unsigned *Mprev, unsigned *Mcur, int r0, int r1)
 {
@@ -508,7 +541,7 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
     const int4 *src = reinterpret_cast<const int4 *>(jb.nbr + (size_t)b0 * dp);
     int4 *dst = reinterpret_cast<int4 *>(st.idx);
     for(int i = threadIdx.x; i < (nr * dp) >> 2; i += ENGINE_THREADS) dst[i] = __ldg(src + i);
-    if(level > 1 && !(jb.flags & GBX_JOB_ACTIVE)){
+    if(level > 1 && !job_active<MODE>(jb)){
       /* saturated lanes at k-1, and at k-2 (Mcur still holds that level's
        * masks; at level 2 it holds nothing of this job) */
       for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS){
@@ -516,7 +549,7 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
         st.act[r] = level >= 3 ? __ldcg(Mcur + b0 + r) : 0u;
       }
     }
-    if(level > 1 && (jb.flags & GBX_JOB_ACTIVE)){
+    if(level > 1 && job_active<MODE>(jb)){
       for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS) st.own[r] = __ldcg(Mprev + b0 + r);
       __syncthreads();
       /* the neighbours' masks: eight independent gathers in flight per thread */
@@ -543,7 +576,7 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
       }
     }
     __syncthreads();
-#define ODP_WC_CASE(L) case L: cnt += run_block<(1 << L)>(st, dp, jb, level, X, Y, Mcur, b0, nr); break;
+#define ODP_WC_CASE(L) case L: cnt += run_block<(1 << L), MODE>(st, dp, jb, level, X, Y, Mcur, b0, nr); break;
     switch(jb.wc_log2){
       ODP_WC_CASE(1) ODP_WC_CASE(2) ODP_WC_CASE(3) ODP_WC_CASE(4)
       ODP_WC_CASE(5) ODP_WC_CASE(6) ODP_WC_CASE(7)
@@ -553,7 +586,7 @@ __device__ unsigned run_rows(Stage &st, const gbx_job &jb, int level, const unsi
     __syncthreads();
     /* saturation masks of this level out; each thread copies the entries it
      * staged, so the next block's staging needs no barrier first */
-    if(level > 1 && !(jb.flags & GBX_JOB_ACTIVE))
+    if(level > 1 && !job_active<MODE>(jb))
       for(int r = threadIdx.x; r < nr; r += ENGINE_THREADS) __stcg(Mcur + b0 + r, st.own[r]);
   }
   return cnt;
@@ -601,6 +634,7 @@ __device__ __forceinline__ bool take_tile(gbx_slot *slots, int nslots, int &curs
   return false;
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(ENGINE_THREADS, ENGINE_MIN_BLOCKS)
 engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int nslots, gbx_ctrl *ctrl,
               gbx_graph_acc *acc, gbx_job_out *job_out, unsigned long long spin_limit_ns)
@@ -689,7 +723,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
        * belongs to the same level and needs no new set-up. */
       unsigned long long pre = 0;
       if(threadIdx.x == 0 && jb.ntiles > 1) pre = atomicAdd(&sl->ticket, 1ull);
-      unsigned cnt = run_rows(sh_stage, jb, level, X, Y, Mprev, Mcur, r0, r1);
+      unsigned cnt = run_rows<MODE>(sh_stage, jb, level, X, Y, Mprev, Mcur, r0, r1);
       cnt = __reduce_add_sync(0xffffffffu, cnt);
       if((threadIdx.x & 31) == 0) sh_warp[threadIdx.x >> 5] = cnt;
       __syncthreads();
@@ -712,7 +746,7 @@ engine_kernel(const gbx_job *__restrict__ jobs, int njobs, gbx_slot *slots, int 
           __threadfence();
           /* level 1 and the full-gather pass count bits set; the pass with
            * change tracking counts bits added */
-          const bool delta = level > 1 && (jb.flags & GBX_JOB_ACTIVE);
+          const bool delta = level > 1 && job_active<MODE>(jb);
           const unsigned long long c = (delta ? vload(&sl->prev) : 0ull) + vload(&sl->count);
           const unsigned long long full = (unsigned long long)jb.n * (unsigned long long)jb.nsrc;
           const bool complete = (c == full);
@@ -869,11 +903,11 @@ __device__ void small_job(const gbx_job &jb, const int *idx, uint4 *b0, uint4 *b
       if(level == 1){
 #pragma unroll
         for(int k = 0; k < S::V; k++) a[k] = make_uint4(0u, 0u, 0u, 0u);
-        mark_source<WC>(a, source_of<SP>(jb.srcpos, r) - src0, nsrc, gl);
+        mark_source<S>(a, source_of<SP>(jb.srcpos, r) - src0, nsrc, gl);
         for(int j = 0; j < dp; j++){
           int u = ip[j];
           if(PART) u = (u >> SMALL_OWNER_SHIFT) * R + (u & SMALL_LOCAL_MASK);
-          mark_source<WC>(a, source_of<SP>(jb.srcpos, u) - src0, nsrc, gl);
+          mark_source<S>(a, source_of<SP>(jb.srcpos, u) - src0, nsrc, gl);
         }
       }
       else{
@@ -1102,10 +1136,16 @@ int gbx_device_init(int *sm_count)
   }
   if(g_engine_blocks == 0){
     int per_sm = 0, per_sm_active = 0;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, STAGE_BYTES_PLAIN);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel<MODE_MIXED>, ENGINE_THREADS,
+                                                      STAGE_BYTES_PLAIN);
     if(e != cudaSuccess) return (int)e;
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_active, engine_kernel, ENGINE_THREADS,
+    int per_sm_a = 0, per_sm_m = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_a, engine_kernel<MODE_ACTIVE>, ENGINE_THREADS,
                                                       STAGE_BYTES_ACTIVE);
+    if(e != cudaSuccess) return (int)e;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm_m, engine_kernel<MODE_MIXED>, ENGINE_THREADS,
+                                                      STAGE_BYTES_ACTIVE);
+    per_sm_active = per_sm_a < per_sm_m ? per_sm_a : per_sm_m;
     if(e != cudaSuccess) return (int)e;
     g_engine_blocks = (per_sm < 1 ? 1 : per_sm) * sms;
     g_engine_blocks_active = (per_sm_active < 1 ? 1 : per_sm_active) * sms;
@@ -1277,9 +1317,14 @@ int gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int n
   if(njobs <= 0 || nslots <= 0) return 0;
   if(blocks <= 0) blocks = gbx_engine_blocks(active);
   if(blocks <= 0) blocks = 1;
-  engine_kernel<<<blocks, ENGINE_THREADS, active ? STAGE_BYTES_ACTIVE : STAGE_BYTES_PLAIN,
-                  (cudaStream_t)stream>>>(d_jobs, njobs, d_slots, nslots, d_ctrl, d_acc, d_job_out,
-                                          spin_limit_ns);
+  const size_t smem = active ? STAGE_BYTES_ACTIVE : STAGE_BYTES_PLAIN;
+  cudaStream_t st = (cudaStream_t)stream;
+  if(active == 1)
+    engine_kernel<MODE_ACTIVE><<<blocks, ENGINE_THREADS, smem, st>>>(d_jobs, njobs, d_slots, nslots, d_ctrl, d_acc,
+                                                                     d_job_out, spin_limit_ns);
+  else
+    engine_kernel<MODE_MIXED><<<blocks, ENGINE_THREADS, smem, st>>>(d_jobs, njobs, d_slots, nslots, d_ctrl, d_acc,
+                                                                    d_job_out, spin_limit_ns);
   return (int)cudaGetLastError();
 }
 
@@ -1397,8 +1442,8 @@ int noalloc_device(NoallocDevice **out)
     if(cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) return ODPX_ERR_CUDA;
     int sms = 0, per_sm = 0;
     if(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return ODPX_ERR_CUDA;
-    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel, ENGINE_THREADS, STAGE_BYTES_PLAIN) !=
-       cudaSuccess)
+    if(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, engine_kernel<MODE_MIXED>, ENGINE_THREADS,
+                                                     STAGE_BYTES_PLAIN) != cudaSuccess)
       return ODPX_ERR_CUDA;
     nd->scratch = (unsigned char *)p;
     nd->blocks = (per_sm < 1 ? 1 : per_sm) * sms;
@@ -1521,7 +1566,7 @@ extern "C" int ODPX_Set_aspl_noalloc(int nodes, int degree, int symmetries, cons
   if(eblocks > 65535LL * 8) eblocks = 65535LL * 8;
   expand_kernel<<<dim3((unsigned)eblocks, (unsigned)((desc.dp + EXPAND_GROUP - 1) / EXPAND_GROUP)), 256, 0, st>>>(
       (const gbx_expand_desc *)(base + off_desc), 1, n, d_err);
-  engine_kernel<<<nd->blocks, ENGINE_THREADS, STAGE_BYTES_PLAIN, st>>>(
+  engine_kernel<MODE_MIXED><<<nd->blocks, ENGINE_THREADS, STAGE_BYTES_PLAIN, st>>>(
       (const gbx_job *)(base + off_jobs), njobs, (gbx_slot *)(base + off_state), nslots,
       (gbx_ctrl *)(base + off_state + out_off), (gbx_graph_acc *)(base + off_state + acc_off),
       (gbx_job_out *)(base + off_state + levels_off), 60ull * 1000000000ull);

@@ -135,11 +135,16 @@ const char *gbx_error_string(int err);
 /* Kernels. */
 int  gbx_expand(const gbx_expand_desc *d_descs, int ndesc, long long total_vertices, int max_dp,
                 unsigned int *d_error, void *stream);
+/* Persistent grid size (SMs x resident CTAs) for the launch's staging size
+ * (active nonzero: some job tracks changes). */
 int  gbx_engine_blocks(int active);
 /* 1 when kernels can read pageable host memory directly (after gbx_device_init). */
-int  gbx_pageable_access(void);    /* persistent grid size (SMs x resident CTAs) for the launch's staging size */
+int  gbx_pageable_access(void);
 /* Streaming read bandwidth of an L2-resident buffer of `bytes` (GB/s). */
 int  gbx_l2_read_probe(size_t bytes, int reps, double *gbs);
+/* The persistent engine over jobs [0, njobs).  active: 0 when no job
+ * tracks changes, 1 when every job does, 2 when some do (each launches an
+ * engine built for exactly those passes). */
 int  gbx_engine_launch(const gbx_job *d_jobs, int njobs, gbx_slot *d_slots, int nslots,
                        gbx_ctrl *d_ctrl, gbx_graph_acc *d_acc, gbx_job_out *d_job_out,
                        unsigned long long spin_limit_ns, int blocks, int active, void *stream);

@@ -551,6 +551,7 @@ int odp_plan_create(const odp_shape *shapes, int count, const odp_tuning *tuning
   for(int k = 0; k < njobs; k++){
     p->h_jobs[k] = jobs[ord[k].job];
     if(p->h_jobs[k].flags & GBX_JOB_ACTIVE) p->any_active = 1;
+    else p->some_plain = 1;
   }
   free(jobs);
   free(ord);
@@ -742,8 +743,8 @@ int odp_plan_enqueue_engine(odp_plan *p)
   }
   return gbx_engine_launch(p->d_jobs, p->njobs, (gbx_slot *)p->d_state, p->nslots,
                            (gbx_ctrl *)(p->d_state + p->out_off), (gbx_graph_acc *)(p->d_state + p->acc_off),
-                           (gbx_job_out *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks, p->any_active,
-                           p->stream);
+                           (gbx_job_out *)(p->d_state + p->levels_off), p->spin_limit_ns, p->blocks,
+                           !p->any_active ? 0 : p->some_plain ? 2 : 1, p->stream);
 }
 
 const gbx_job_out *odp_plan_job_out(const odp_plan *p)

@@ -70,6 +70,7 @@ typedef struct odp_plan {
   unsigned long long spin_limit_ns;
   int blocks;
   int any_active;              /* some job tracks changes: launch with the full staging area */
+  int some_plain;              /* some job does not (with any_active: the engine built for both) */
   double bytes_alg_last;       /* algorithmic bytes of the last run (roofline) */
   int reordered;               /* the job order was learned from a run */
   int direct;                  /* the device pulls the callers' arrays (h_expand holds their pointers) */
