@@ -232,6 +232,7 @@ struct RowShape {
   static constexpr int G = VPR < 32 ? VPR : 32;      /* lanes per row */
   static constexpr int V = VPR / G;                  /* vectors per lane */
   static constexpr int RPW = 32 / G;                 /* rows per warp pass */
+  static constexpr bool LEAN = false;                /* change tests by comparing words */
 };
 
 /* The shape of the change-tracking passes when every job of a plan tracks
@@ -245,6 +246,7 @@ struct RowShapeWide {
   static constexpr int G = VPR >= 64 ? 32 : (VPR >= 2 ? VPR / 2 : 1);
   static constexpr int V = VPR / G;
   static constexpr int RPW = 32 / G;
+  static constexpr bool LEAN = true;                 /* change tests by popcount: words only grow */
 };
 
 /* Set local source bit b (0 <= b < nsrc) if it lands in this lane's vectors. */
@@ -321,12 +323,22 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
     bool changed = false;
     if(valid){
       const int row = row0 + r;
-      uint4 acc[S::V], id[S::V];
+      constexpr bool IDW = ACT && !S::LEAN;             /* the identity kept as words */
+      uint4 acc[S::V], id[IDW ? S::V : 1];
 #pragma unroll
-      for(int k = 0; k < S::V; k++){ acc[k] = make_uint4(0u, 0u, 0u, 0u); id[k] = acc[k]; }
+      for(int k = 0; k < S::V; k++) acc[k] = make_uint4(0u, 0u, 0u, 0u);
       const int self = source_of<SP>(jb.srcpos, row) - src0;
       mark_source<S>(acc, self, nsrc, gl);
-      if(ACT) mark_source<S>(id, self, nsrc, gl);
+      if(IDW){
+#pragma unroll
+        for(int k = 0; k < S::V; k++) id[k] = acc[k];
+      }
+      /* LEAN: the identity's bits in this lane (0 or 1) */
+      unsigned id_bits = 0;
+      if(ACT && S::LEAN){
+#pragma unroll
+        for(int k = 0; k < S::V; k++) id_bits += popc4(acc[k]);
+      }
       const int4 *ip = reinterpret_cast<const int4 *>(st.idx + r * dp);
       for(int j = 0; j < (dp >> 2); j++){
         int4 q = ip[j];
@@ -341,10 +353,11 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
       for(int k = 0; k < S::V; k++){
         __stcg(yr + k * S::G, acc[k]);
         c += popc4(acc[k]);
-        if(ACT)
+        if(IDW)
           changed |= (acc[k].x != id[k].x) | (acc[k].y != id[k].y) | (acc[k].z != id[k].z) |
                      (acc[k].w != id[k].w);
       }
+      if(ACT && S::LEAN) changed = c != id_bits;
       cnt += c;
       if(!ACT) changed = c == (unsigned)lane_sources<WC>(nsrc, gl);    /* saturated */
     }
@@ -430,7 +443,7 @@ __device__ unsigned rows_levelk_all(Stage &st, int dp, int d, int nsrc, const un
  * its words differ from that (changed at k-1 or at k), except at level 2,
  * where Y has never been written and every word is stored.  Returns the bits
  * added at this level; the row's new change mask goes to Mcur. */
-template <int WC, class S = RowShape<WC>>
+template <int WC, class S = RowShape<WC>, bool LEAN = S::LEAN>
 __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long long *X, unsigned long long *Y,
                                 unsigned *Mcur, int row0, int nrows, bool write_all)
 {
@@ -446,10 +459,17 @@ __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long lon
     if(valid && (write_all || ((st.act[r] >> gl) & 1u))){
       const int row = row0 + r;
       const bool own = (st.own[r] >> gl) & 1u;
-      uint4 acc[S::V], old[S::V];
+      /* LEAN: the words only grow, so they changed exactly when their
+       * popcount did; the previous words need not be kept */
+      uint4 acc[S::V], old[LEAN ? 1 : S::V];
+      unsigned pold = 0;
       const uint4 *xr = Xv + (size_t)row * S::VPR + gl;
 #pragma unroll
-      for(int k = 0; k < S::V; k++){ old[k] = __ldcg(xr + k * S::G); acc[k] = old[k]; }
+      for(int k = 0; k < S::V; k++){
+        acc[k] = __ldcg(xr + k * S::G);
+        if(LEAN) pold += popc4(acc[k]);
+        else old[k] = acc[k];
+      }
       const int *ip = st.idx + r * dp;
       const unsigned *mp = st.nmask + r * dp;
       for(int j = 0; j < dp; j += NB){
@@ -469,11 +489,19 @@ __device__ unsigned rows_levelk(const Stage &st, int dp, const unsigned long lon
           for(int k = 0; k < S::V; k++) or_into(acc[k], t[i][k]);
       }
       unsigned added = 0;
+      if(LEAN){
 #pragma unroll
-      for(int k = 0; k < S::V; k++){
-        added += popc4(acc[k]) - popc4(old[k]);
-        changed |= (acc[k].x != old[k].x) | (acc[k].y != old[k].y) | (acc[k].z != old[k].z) |
-                   (acc[k].w != old[k].w);
+        for(int k = 0; k < S::V; k++) added += popc4(acc[k]);
+        added -= pold;
+        changed = added != 0;
+      }
+      else{
+#pragma unroll
+        for(int k = 0; k < S::V; k++){
+          added += popc4(acc[k]) - popc4(old[k]);
+          changed |= (acc[k].x != old[k].x) | (acc[k].y != old[k].y) | (acc[k].z != old[k].z) |
+                     (acc[k].w != old[k].w);
+        }
       }
       if(own || changed || write_all){
         uint4 *yr = reinterpret_cast<uint4 *>(Y) + (size_t)row * S::VPR + gl;
