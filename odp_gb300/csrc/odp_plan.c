@@ -275,19 +275,21 @@ static void fill_state_init(odp_plan *p)
 
 /* Whether a graph's jobs track changes (gather only words that changed at
  * the previous level).  It is exact for every graph.  Without it, lanes whose
- * words are saturated already skip their gathers, and on GB300 the per-row
- * staging of change tracking, and in a batch the larger staging area of
- * every job, cost more than it saves, except on large grids with many
- * sources evaluated alone.  Measured against the saturation skip alone:
- * 256 x 256 grid, d = 6, diameter 140: 28.3 -> 25.3 ms; 224 x 224: 18.2 ->
- * 15.7 ms; 256 x 256, d = 8, s = 2 (32768 sources): 9.7 -> 9.1 ms; but
- * 256 x 256, s = 4 (16384 sources, so only four 64-word jobs): 7.3 -> 8.2 ms;
- * and before the skip already +5 % to +21 % on single grids of 64 x 64 to
- * 180 x 180 and +8 % on the 512-graph batch.  So by default it is on only for
- * a single grid of at least 49152 vertices and 32768 sources. */
+ * words are saturated already skip their gathers; with it, every row stages
+ * its neighbours' change masks, which pays where levels are many and each
+ * changes few words: single grids.  Plans whose every job tracks changes run
+ * the engine built for those passes alone, with two vectors per lane.
+ * Measured on GB300, on against off (ms): 100 x 100, d = 4: 1.27 / 1.10;
+ * 128 x 128, d = 6: 1.63 / 1.42, but d = 4: 1.87 / 2.04; 160 x 160: 3.62 /
+ * 3.96; 192 x 192: 6.26 / 9.15; 224 x 224: 12.9 / 17.4; 256 x 256, s = 4:
+ * 6.86 / 7.04; 256 x 256, d = 8, s = 2: 9.76 / 13.3.  In batches the larger
+ * staging area of every job cost more than it saved (the 512-graph batch:
+ * 9.0 against 7.15 ms tuned).  So by default it is on for a single grid of
+ * at least 20000 vertices. */
 static int tracks_changes(const odp_tuning *t, int count, int grid, int n, int s)
 {
-  if(t->activity == -2) return count == 1 && grid && n >= 49152 && n / s >= 32768;
+  (void)s;
+  if(t->activity == -2) return count == 1 && grid && n >= 20000;
   return t->activity == -1 ? grid : t->activity;
 }
 
