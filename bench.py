@@ -72,9 +72,9 @@ BATCH_SHA256 = "cb594241cefc45d1"
 # G the configuration graphs with the default schedule.  A launch's L2 read
 # bytes and DRAM traffic are taken as its algorithmic bytes times these ratios.
 NCU_RATIOS = {
-    "batch": {"l2_read": 0.572758, "dram": 0.108146},
-    "C2": {"l2_read": 0.654676, "dram": 0.108437},
-    "C3": {"l2_read": 0.784851, "dram": 0.205265},
+    "batch": {"l2_read": 0.641194, "dram": 0.092754},
+    "C2": {"l2_read": 0.654699, "dram": 0.106574},
+    "C3": {"l2_read": 0.784801, "dram": 0.145122},
     "G": {"l2_read": 0.261177, "dram": 0.095565},
 }
 
