@@ -241,8 +241,10 @@ struct RowShape {
  * GB300 it cut the 512-graph batch from 6.90 to 6.21 ms (tuned), the
  * n = 65536 graph from 2.81 to 2.60 ms and the 256 x 256 grid, where few
  * neighbours of a row change per level, from 21.2 to 18.4 ms.  (RowShape,
- * one vector per lane up to 32 lanes per row, remains for the small-graph
- * kernel and for change-tracking jobs in plans that mix both kinds.) */
+ * one vector per lane up to 32 lanes per row, remains for change-tracking
+ * jobs in plans that mix both kinds and for the small-graph kernel, where
+ * two vectors per lane made the partitioned grids 10-33 % slower: their
+ * gathers from other CTAs' shared memory go one 16-byte request at a time.) */
 template <int WC>
 struct RowShapeWide {
   static constexpr int VPR = WC / 2;
